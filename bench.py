@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Benchmark of the netcalc hot path on GB300.
+
+Workload (the large single-system configuration): all-pairs generalized
+correlation of a synthetic protein trajectory with N = 2000 nodes,
+m = 10000 frames, d = 3, k = 6 (1,999,000 node pairs in total). A step is
+one batch of `--pairs-per-step` consecutive pairs of that all-pairs list;
+different steps (and ranks) take different batches. The trajectory stays
+resident in HBM (X = 2000 x 3 x 10048 floats, 241 MB, larger than the
+129 MB L2, so every step streams it from HBM).
+
+Lines reported (one JSON line from rank 0):
+  value     pairs/s of the batched persistent plan (graph replay), device
+            timed with CUDA events, max over ranks; inputs resident.
+  e2e       pairs/s through the drop-in API (netcalc.generalizedCorrelation
+            over host CuArrays): host->device upload of X and the pair list
+            and device->host read of the results inside every step.
+  plain_per_call  pairs/s of one netcalc.generalizedCorrelationGpu call per
+            pair (the reference's call structure) on a small sample.
+  apsp      Hedetniemi shortest-path ms on N = 2000 random geometric graphs
+            (mean degree 12), integer weights U[1,100] and float weights.
+  roofline  the count kernel against the CUDA-core issue peak (SMs x 128
+            lanes x max SM clock); algorithmic work per pair
+            8*d*m*(m-1) FP32 ops.
+  cpu_baseline  the CPU oracle port (restatement of the reference CPU path)
+            on all host cores, on a bounded sample of pairs of this workload.
+
+``--impl reference`` runs only the CPU oracle port arm and prints its line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "netsci_gb300" / "dropin"))
+
+N_NODES, M_FRAMES, DIM, K_NN = 2000, 10000, 3, 6
+SEED = 2000
+METRIC = "GC pairs/sec (batched persistent), N=2000 nodes, m=10000 frames"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--pairs-per-step", type=int, default=8192)
+    p.add_argument("--quick", action="store_true", help="small problem, for debugging")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--cpu-sample", type=int, default=0, help="pairs in the CPU baseline sample")
+    return p.parse_args()
+
+
+def workload(quick: bool):
+    from netsci_gb300 import synthetic
+    if quick:
+        N, m = 200, 2000
+    else:
+        N, m = N_NODES, M_FRAMES
+    X, mean = synthetic.protein_trajectory(N, m, seed=SEED)
+    return X, mean, N, m
+
+
+def ops_per_pair(m: int, d: int = DIM) -> float:
+    return 8.0 * d * m * (m - 1)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                    timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 4 + i and s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def cpu_baseline(X, m, ab, threads: int):
+    """The oracle port on `threads` host threads over len(ab) pairs."""
+    import oracle
+    t0 = time.perf_counter()
+    oracle.pairs(X, m, DIM, ab, K_NN, gc=True, threads=threads)
+    dt = time.perf_counter() - t0
+    return len(ab) / dt, dt
+
+
+def reference_arm(args, rank: int):
+    if rank != 0:
+        return
+    X, mean, N, m = workload(args.quick)
+    from netsci_gb300 import synthetic
+    ab_all = synthetic.all_pairs(N)
+    threads = os.cpu_count() or 1
+    per_step = args.cpu_sample or threads
+    rng = np.random.default_rng(7)
+    times = []
+    for s in range(args.warmup + args.steps):
+        sel = ab_all[rng.choice(len(ab_all), size=per_step, replace=False)]
+        rate, dt = cpu_baseline(X, m, sel, threads)
+        if s >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = per_step * args.steps / total
+    line = {
+        "metric": METRIC, "impl": "reference", "value": value, "unit": "pairs/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"all-pairs GC, N={N} nodes, m={m} frames, d={DIM}, k={K_NN}",
+                   "pairs_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} random pairs per step, one per thread"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from netsci_gb300 import device, synthetic
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v: float) -> float:
+        if world == 1:
+            return v
+        t = torch.tensor([v], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    X, mean, N, m = workload(args.quick)
+    ab_all = synthetic.all_pairs(N)
+    B = args.pairs_per_step
+    S = args.warmup + args.steps
+    need = world * S * B
+    if need > len(ab_all):
+        raise SystemExit(f"{need} pairs requested, the workload has {len(ab_all)}")
+
+    Xd, mm = device.pack_trajectory(X, DIM)
+    torch.cuda.synchronize()
+
+    def slice_for(step: int) -> np.ndarray:
+        off = (rank * S + step) * B
+        return ab_all[off:off + B]
+
+    # ---- batched persistent plans (graph + kernel events) --------------------
+    outs, plans = [], []
+    for s in range(S):
+        gc = torch.empty(B, device="cuda")
+        plans.append(device.KsgPlan(device.make_pairs(Xd, mm, slice_for(s)), K_NN, DIM, gc=gc,
+                                    graph=True, timing=True))
+        outs.append(gc)
+    for s in range(args.warmup):
+        plans[s].run()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record()
+        for s in range(args.warmup, S):
+            plans[s].run()
+        ev1.record()
+        torch.cuda.synchronize()
+    barrier()
+    dev_ms = ev0.elapsed_time(ev1)
+    count_ms = [plans[s].count_ms() for s in range(args.warmup, S)]
+    launches = sum(plans[s].launches for s in range(args.warmup, S))
+    t_max = max_over_ranks(dev_ms) / 1000.0
+    value = world * args.steps * B / t_max
+    gc_vals = torch.cat([outs[s] for s in range(args.warmup, S)]).cpu().numpy()
+    assert np.all(np.isfinite(gc_vals)) and np.all((gc_vals >= 0) & (gc_vals <= 1))
+
+    # ---- roofline of the count kernel ------------------------------------------
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    props = torch.cuda.get_device_properties(local)
+    sm_max = float(peaks.get("sm_max_mhz") or 2070.0)
+    peak_gops = props.multi_processor_count * 128 * sm_max * 1e6 / 1e9
+    ops_launch = ops_per_pair(m) * B
+    avg_launch_s = statistics.mean(count_ms) / 1000.0
+    achieved = ops_launch / avg_launch_s / 1e9
+    clocks = clk.summary()
+    frac_at_clock = None
+    if clocks.get("sm_mhz"):
+        frac_at_clock = achieved / (props.multi_processor_count * 128 * clocks["sm_mhz"] * 1e6 / 1e9)
+
+    # ---- e2e through the drop-in CuArray API -------------------------------------
+    e2e = None
+    if not args.no_e2e:
+        import cuarray
+        import netcalc
+        Xc = cuarray.FloatCuArray()
+        Xc.fromNumpy2D(X)
+        abs_ = []
+        for s in range(S):
+            a = cuarray.IntCuArray()
+            a.fromNumpy2D(slice_for(s))
+            abs_.append(a)
+        R = cuarray.FloatCuArray()
+        for s in range(args.warmup):
+            netcalc.generalizedCorrelation(X=Xc, R=R, ab=abs_[s], k=K_NN, n=m, xd=2, d=DIM,
+                                           platform=0)
+        barrier()
+        t0 = time.perf_counter()
+        for s in range(args.warmup, S):
+            netcalc.generalizedCorrelation(X=Xc, R=R, ab=abs_[s], k=K_NN, n=m, xd=2, d=DIM,
+                                           platform=0)
+        torch.cuda.synchronize()
+        dt = max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": world * args.steps * B / dt, "unit": "pairs/s",
+               "h2d_bytes_per_step": int(X.nbytes + B * 2 * 4),
+               "d2h_bytes_per_step": int(B * 4),
+               "api": "netcalc.generalizedCorrelation over host CuArrays (pageable host memory)"}
+        last = R.toNumpy1D()
+        assert np.array_equal(last, outs[S - 1].cpu().numpy()) or \
+            np.max(np.abs(last - outs[S - 1].cpu().numpy())) <= 1e-6
+
+    # ---- plain per-call (the reference's call structure) ------------------------
+    plain = None
+    if rank == 0:
+        import cuarray
+        import netcalc
+        sample = 16 if not args.quick else 8
+        rows = slice_for(0)[:sample]
+        xs = []
+        for a, b in rows:
+            xa, xb = cuarray.FloatCuArray(), cuarray.FloatCuArray()
+            xa.fromNumpy1D(X[a])
+            xb.fromNumpy1D(X[b])
+            xs.append((xa, xb))
+        netcalc.generalizedCorrelationGpu(Xa=xs[0][0], Xb=xs[0][1], k=K_NN, n=m, xd=2, d=DIM)
+        t0 = time.perf_counter()
+        for xa, xb in xs:
+            netcalc.generalizedCorrelationGpu(Xa=xa, Xb=xb, k=K_NN, n=m, xd=2, d=DIM)
+        dt = time.perf_counter() - t0
+        plain = {"value": sample / dt, "unit": "pairs/s", "sample": f"{sample} pairs, one call each"}
+
+    # ---- APSP ------------------------------------------------------------------------
+    apsp = None
+    if rank == 0:
+        apsp = {}
+        n_g = 2000 if not args.quick else 500
+        for name, integer in (("rgg_int", True), ("rgg_float", False)):
+            A = torch.from_numpy(synthetic.random_geometric_graph(n_g, 12, seed=11,
+                                                                  integer_weights=integer)).cuda()
+            device.apsp_lengths(A, n_g)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            H, steps = device.apsp_lengths(A, n_g)
+            torch.cuda.synchronize()
+            apsp[f"{name}_ms"] = 1000 * (time.perf_counter() - t0)
+            apsp[f"{name}_steps"] = steps
+        apsp["n"] = n_g
+
+    # ---- CPU baseline (oracle port on host cores) --------------------------------------
+    cpu = None
+    if rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        n_s = args.cpu_sample or threads
+        sel = ab_all[np.random.default_rng(3).choice(len(ab_all), size=n_s, replace=False)]
+        rate, dt = cpu_baseline(X, m, sel, threads)
+        cpu = {"value": rate, "unit": "pairs/s", "cores": threads, "kind": "port",
+               "sample": f"{n_s} random pairs of the workload, {dt:.1f} s wall"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"all-pairs GC, N={N} nodes, m={m} frames, d={DIM}, k={K_NN}",
+                       "pairs_per_step": B, "total_pairs": int(len(ab_all)),
+                       "parallelism": f"pairs sharded over {world} GPU(s), no collective",
+                       "l2": "inputs larger than L2 (X resident, 241 MB > 129 MB L2)",
+                       "tile": None},
+            "e2e": e2e, "plain_per_call": plain, "apsp": apsp,
+            "gpu_launches": launches,
+            "roofline": {"bound": "cuda_core_issue", "achieved": achieved,
+                         "peak": peak_gops, "unit": "Gop/s", "frac": achieved / peak_gops,
+                         "frac_at_median_clock": frac_at_clock, "traffic": None,
+                         "kernel": "ksg_count_kernel",
+                         "ops_per_launch": ops_launch,
+                         "peak_source": (f"{props.multi_processor_count} SMs x 128 lanes x "
+                                         f"{sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)")},
+            "cpu_baseline": cpu, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    for p in plans:
+        p.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

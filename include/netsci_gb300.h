@@ -1,0 +1,217 @@
+/*
+ * netsci_gb300 C ABI.
+ *
+ * The drop-in boundary for NetSci's netcalc hot path (KSG mutual
+ * information, generalized correlation, Hedetniemi all-pairs shortest
+ * paths) on one GB300 GPU. Plain C types only: opaque handles, pointers and
+ * sizes. Every function returns an nsg status (NSG_OK == 0); on failure
+ * nsg_last_error() gives a message for the calling thread.
+ *
+ * Three layers:
+ *   1. CuArray handles: the reference's CuArray<T> container
+ *      (cuarray/include/cuarray.h:23-489), for FFI callers (ctypes, cffi,
+ *      SWIG-less bindings).
+ *   2. netcalc calls over CuArray handles, one per reference function
+ *      (netcalc/include/{mutual_information,generalized_correlation,
+ *      hedetniemi,psi,math_utils}.h), same argument meaning, same return
+ *      values, invalid platform -> NSG_ERR_PLATFORM.
+ *   3. Device-pointer entry points (stream-explicit, caller-owned device
+ *      buffers) for batched and resident workloads; these have no single
+ *      reference counterpart and say which reference loop they replace.
+ *
+ * Device pointers are CUDA device addresses on the current device. Streams
+ * are cudaStream_t passed as void* (NULL = legacy default stream).
+ */
+#ifndef NETSCI_GB300_H
+#define NETSCI_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NSG_OK 0
+#define NSG_ERR_INVALID 1       /* invalid argument                         */
+#define NSG_ERR_CUDA 2          /* CUDA runtime error                       */
+#define NSG_ERR_PLATFORM 3      /* platform not 0 (GPU) or 1 (CPU)          */
+#define NSG_ERR_UNSUPPORTED 4   /* valid but not supported (e.g. k > 32)    */
+#define NSG_ERR_DEVICE_FAULT 5  /* a kernel's bounded wait ran out          */
+#define NSG_ERR_IO 6            /* file read/write failure                  */
+
+#define NSG_DTYPE_FLOAT32 0
+#define NSG_DTYPE_INT32 1
+#define NSG_DTYPE_FLOAT64 2
+
+/* Platform constants of netcalc/include/platform.h:8-11. */
+#define NSG_GPU_PLATFORM 0
+#define NSG_CPU_PLATFORM 1
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* nsg_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int nsg_version(void);
+/* Frees memory returned by the library (nsg_recover_single_shortest_path). */
+void nsg_free(void* p);
+
+/* ---- 1. CuArray handles (cuarray/include/cuarray.h:23-489) -------------- */
+typedef struct nsg_cuarray nsg_cuarray;
+
+/* new CuArray<T>() / delete (cuarray/src/cuarray.cu:8-14, :65-73) */
+int nsg_cuarray_create(int dtype, nsg_cuarray** out);
+int nsg_cuarray_destroy(nsg_cuarray* a);
+int nsg_cuarray_dtype(const nsg_cuarray* a);
+/* init(m, n): zero-filled host buffer (cuarray.h:49) */
+int nsg_cuarray_init(nsg_cuarray* a, int m, int n, int* cuarray_error);
+/* init(host, m, n): copy of a host buffer (cuarray.h:68) */
+int nsg_cuarray_init_from(nsg_cuarray* a, const void* host, int m, int n, int* cuarray_error);
+/* fromCuArrayShallowCopy / fromCuArrayDeepCopy (cuarray.h:91, :116) */
+int nsg_cuarray_from_cuarray_shallow(nsg_cuarray* a, nsg_cuarray* src, int start, int end,
+                                     int m, int n, int* cuarray_error);
+int nsg_cuarray_from_cuarray_deep(nsg_cuarray* a, nsg_cuarray* src, int start, int end, int m,
+                                  int n, int* cuarray_error);
+/* fromNumpy 1-D (m = 1) and 2-D (cuarray.h:297, :315): copies `data` */
+int nsg_cuarray_from_host(nsg_cuarray* a, const void* data, int m, int n, int* cuarray_error);
+/* m(), n(), size(), bytes(), owner(), allocatedHost(), allocatedDevice() */
+int nsg_cuarray_shape(const nsg_cuarray* a, int* m, int* n, int* size, size_t* bytes,
+                      int* owner, int* allocated_host, int* allocated_device);
+/* host() / device() raw pointers (cuarray.h:190, :200) */
+void* nsg_cuarray_host(nsg_cuarray* a);
+void* nsg_cuarray_device(nsg_cuarray* a);
+/* allocateHost, allocateDevice, toDevice, toHost, deallocateHost,
+ * deallocateDevice (cuarray.h:211-282); *cuarray_error is the CuArrayError */
+int nsg_cuarray_allocate_host(nsg_cuarray* a, int* cuarray_error);
+int nsg_cuarray_allocate_device(nsg_cuarray* a, int* cuarray_error);
+int nsg_cuarray_to_device(nsg_cuarray* a, int* cuarray_error);
+int nsg_cuarray_to_host(nsg_cuarray* a, int* cuarray_error);
+int nsg_cuarray_deallocate_host(nsg_cuarray* a, int* cuarray_error);
+int nsg_cuarray_deallocate_device(nsg_cuarray* a, int* cuarray_error);
+/* get(i, j) / set(value, i, j) (cuarray.h:365, :383); values as double */
+int nsg_cuarray_get(const nsg_cuarray* a, int i, int j, double* value);
+int nsg_cuarray_set(nsg_cuarray* a, double value, int i, int j, int* cuarray_error);
+/* load / save .npy (cuarray.h:399, :410) */
+int nsg_cuarray_load(nsg_cuarray* a, const char* path, int* cuarray_error);
+int nsg_cuarray_save(nsg_cuarray* a, const char* path);
+/* sort(i) (descending copy of row i) and argsort(i) (cuarray.h:422, :458) */
+int nsg_cuarray_sort(nsg_cuarray* a, int i, nsg_cuarray** out);
+int nsg_cuarray_argsort(nsg_cuarray* a, int i, nsg_cuarray** out);
+
+/* ---- 2. netcalc over CuArray handles ------------------------------------ */
+/* X: N x (d*n) float, plane-major node rows; ab: P x 2 int; I/R: re-inited
+ * to 1 x P. *result is the reference's return value (the platform).       */
+/* netcalc/include/mutual_information.h:34-43 (plain), :20-31 (checkpoint) */
+int nsg_mutual_information(nsg_cuarray* X, nsg_cuarray* I, nsg_cuarray* ab, int k, int n,
+                           int xd, int d, int platform, int* result);
+int nsg_mutual_information_checkpointed(nsg_cuarray* X, nsg_cuarray* I, nsg_cuarray* ab, int k,
+                                        int n, int xd, int d, int platform,
+                                        int checkpoint_frequency,
+                                        const char* checkpoint_file_name, int* result);
+/* netcalc/include/mutual_information.h:45-66 (per-pair GPU / CPU) */
+int nsg_mutual_information_gpu(nsg_cuarray* Xa, nsg_cuarray* Xb, int k, int n, int xd, int d,
+                               float* result);
+int nsg_mutual_information_cpu(nsg_cuarray* Xa, nsg_cuarray* Xb, int k, int n, int xd, int d,
+                               float* result);
+/* netcalc/include/generalized_correlation.h:55-64 (plain), :30-53 (ckpt) */
+int nsg_generalized_correlation(nsg_cuarray* X, nsg_cuarray* R, nsg_cuarray* ab, int k, int n,
+                                int xd, int d, int platform, int* result);
+int nsg_generalized_correlation_checkpointed(nsg_cuarray* X, nsg_cuarray* R, nsg_cuarray* ab,
+                                             int k, int n, int xd, int d, int platform,
+                                             int checkpoint_frequency,
+                                             const char* checkpoint_file_name, int* result);
+/* netcalc/include/generalized_correlation.h:66-96 (per-pair GPU / CPU) */
+int nsg_generalized_correlation_gpu(nsg_cuarray* Xa, nsg_cuarray* Xb, int k, int n, int xd,
+                                    int d, float* result);
+int nsg_generalized_correlation_cpu(nsg_cuarray* Xa, nsg_cuarray* Xb, int k, int n, int xd,
+                                    int d, float* result);
+/* netcalc/include/mutual_information.h:68-80 */
+int nsg_generate_restart_ab_from_checkpoint_file(nsg_cuarray* ab, nsg_cuarray* restart_ab,
+                                                 const char* checkpoint_file_name);
+/* netcalc/include/hedetniemi.h:31-38, :60-66, :106-111, :122-126 */
+int nsg_hedetniemi_all_shortest_paths(nsg_cuarray* A, nsg_cuarray* H, nsg_cuarray* paths,
+                                      int max_path_length, float tolerance, int platform);
+int nsg_hedetniemi_all_shortest_paths_gpu(nsg_cuarray* A, nsg_cuarray* H, nsg_cuarray* paths,
+                                          float tolerance, int max_path_length);
+int nsg_hedetniemi_all_shortest_path_lengths(nsg_cuarray* A, nsg_cuarray* H,
+                                             int max_path_length, int platform);
+int nsg_hedetniemi_all_shortest_path_lengths_gpu(nsg_cuarray* A, nsg_cuarray* H,
+                                                 int max_path_length);
+/* netcalc/include/hedetniemi.h:139-160 */
+int nsg_correlation_to_adjacency(nsg_cuarray* A, nsg_cuarray* C, int n, int platform);
+/* netcalc/include/hedetniemi.h:173-180: *path (free with nsg_free), *len */
+int nsg_recover_single_shortest_path(nsg_cuarray* paths, int max_path_length, int i, int j,
+                                     int** path, int* len);
+/* netcalc/include/psi.h:160-163 (generatePsi, table of n+1 floats) */
+int nsg_generate_psi(nsg_cuarray* psi, int n);
+
+/* ---- 3. device-pointer entry points -------------------------------------- */
+
+/* One KSG variable pair on the device. Component c of sample s of variable
+ * a is xa[c*ld + f(s)] with f the identity, or f(s) = fmap[s] (bootstrap
+ * resample; fmap a device int array of m frame indices < ld).            */
+typedef struct nsg_ksg_pair {
+    const float* xa;
+    const float* xb;
+    const int* fmap;
+    int ld;
+    int m;
+} nsg_ksg_pair;
+
+/* All pairs of a list in one persistent launch plus a finalize launch.
+ * Replaces the per-pair loop of netcalc/src/generalized_correlation.cpp:
+ * 104-173 and netcalc/src/mutual_information.cpp:103-172 together with the
+ * per-pair GPU call of netcalc/src/mutual_information_gpu.cu:1007-1079.
+ * pairs: host array. mi / gc / w: device float[npairs] outputs, each
+ * nullable (w = -ln(gc), +inf where gc == 0). Asynchronous on `stream`.  */
+int nsg_ksg_pairs_device(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi,
+                         float* gc, float* w, void* stream);
+
+/* One pair with per-sample outputs (device arrays of m, each nullable):
+ * marginal counts n_x, n_y (after the reference's -1), eps_x, eps_y and the
+ * k-th neighbour joint distance. mi: device float[1], nullable.            */
+int nsg_ksg_pair_detail_device(const float* xa, const float* xb, int ld, int m, int k, int d,
+                               int* n_x, int* n_y, float* eps_x, float* eps_y, float* kdist,
+                               float* mi, void* stream);
+
+/* Reusable plan: device descriptors, work queue and scratch built once;
+ * each run is one captured CUDA graph (work-queue reset, count kernel,
+ * finalize kernel per batch). Flags: bit 0 = capture a CUDA graph; bit 1 =
+ * record CUDA events around every count launch (nsg_ksg_plan_count_ms).
+ * The tile shape comes from the autotuner cache when one is loaded.       */
+typedef struct nsg_ksg_plan nsg_ksg_plan;
+int nsg_ksg_plan_create(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi,
+                        float* gc, float* w, int flags, nsg_ksg_plan** out);
+int nsg_ksg_plan_run(nsg_ksg_plan* plan, void* stream);
+/* Kernel launches one run makes (count + finalize per batch). */
+int nsg_ksg_plan_launches(const nsg_ksg_plan* plan, int* launches);
+/* Device milliseconds of the count kernels in the last run (flag bit 1);
+ * waits for that run's events.                                          */
+int nsg_ksg_plan_count_ms(const nsg_ksg_plan* plan, float* ms);
+int nsg_ksg_plan_destroy(nsg_ksg_plan* plan);
+
+/* Force a KSG tile shape (CTA threads, samples per thread, frames per tile,
+ * arithmetic variant; variant < 0 = any) for subsequent calls in this
+ * process; threads == 0 restores automatic choice.                        */
+int nsg_ksg_set_shape(int threads, int r, int frames, int variant);
+
+/* Hedetniemi shortest path lengths on the device (A, H: n x n device
+ * floats). H_{t+1}[i][j] = min_k A[j][k] + H_t[k][i] from H_0 = A, until H
+ * stops changing or max_path_length steps; the steps run go to *steps
+ * (host, nullable). netcalc/src/hedetniemi_gpu.cu:109-146. Synchronizes
+ * `stream` once at the end to read the step count.                       */
+int nsg_apsp_lengths_device(const float* A, float* H, int n, int max_path_length, int* steps,
+                            void* stream);
+/* Shortest paths with snapshots: paths device int[n*max_path_length*n],
+ * layout paths[i*L*n + j*L + p]. netcalc/src/hedetniemi_gpu.cu:148-235. */
+int nsg_apsp_paths_device(const float* A, float* H, int* paths, int n, int max_path_length,
+                          float tolerance, void* stream);
+/* Correlation -> adjacency on the device: mode 0 = 1/r with +inf for r == 0
+ * (netcalc/src/hedetniemi_gpu.cu:10-26); mode 1 = -ln(r) with +inf for
+ * r <= 0. Diagonal 0 in both.                                             */
+int nsg_corr_to_adjacency_device(const float* C, float* A, int n, int mode, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NETSCI_GB300_H */

@@ -1,0 +1,266 @@
+// Hedetniemi all-pairs shortest paths on the GPU.
+//
+// One step computes, for every (i, j),
+//     Hn[i][j] = min_k fl(A[j][k] + H[k][i])
+// the update of netcalc/src/hedetniemi_gpu.cu:28-45, as a Jacobi step from H
+// into a second buffer (the reference updates H in place). Every entry is a
+// minimum of single roundings, so the result does not depend on the order k
+// is visited in and matches the CPU restatement bit for bit.
+//
+// Kernel shape: a 128 x 128 output tile per CTA of 256 threads, 8 x 8 outputs
+// per thread, k in slabs of 16 staged in shared memory as interleaved pairs
+// (k, k+1), so one packed add (add.rn.f32x2) forms two candidate sums and one
+// three-input min folds both into the running minimum: two instructions per
+// two (i, j, k) terms. The work is FADD/FMNMX issue-bound on CUDA cores; a
+// min-plus product has no tensor-core form.
+//
+// Convergence: step t writes changed[t] = 1 when any entry differs from H;
+// step t+1 returns at once when changed[t] == 0 (H is then a fixed point and
+// both buffers hold it).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "apsp.h"
+#include "common.cuh"
+
+namespace nsg {
+namespace {
+
+constexpr int kTile = 128;
+constexpr int kSlab = 16;  // k values per stage (8 pairs)
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    unsigned long long ra, rb, rr;
+    ra = (static_cast<unsigned long long>(__float_as_uint(a.y)) << 32) | __float_as_uint(a.x);
+    rb = (static_cast<unsigned long long>(__float_as_uint(b.y)) << 32) | __float_as_uint(b.x);
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(rr) : "l"(ra), "l"(rb));
+    return make_float2(__uint_as_float(static_cast<unsigned>(rr & 0xffffffffu)),
+                       __uint_as_float(static_cast<unsigned>(rr >> 32)));
+}
+
+__global__ void __launch_bounds__(kThreads)
+hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
+                       float* __restrict__ Hn, int n, int* changed, int step) {
+    if (step > 0 && changed[step - 1] == 0) return;  // fixed point reached earlier
+    __shared__ __align__(16) float2 Hs[kSlab / 2][kTile];  // (H[k][i], H[k+1][i])
+    __shared__ __align__(16) float2 As[kSlab / 2][kTile];  // (A[j][k], A[j][k+1])
+    const float inf = __int_as_float(0x7f800000);
+    const int tid = threadIdx.x;
+    const int tx = tid & 15;   // i direction
+    const int ty = tid >> 4;   // j direction
+    const int i0 = blockIdx.y * kTile;
+    const int j0 = blockIdx.x * kTile;
+
+    float acc[8][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = inf;
+
+    for (int k0 = 0; k0 < n; k0 += kSlab) {
+        __syncthreads();
+        // H slab: rows k0..k0+15, columns i0..i0+127 (coalesced along i)
+#pragma unroll
+        for (int e = 0; e < (kSlab * kTile) / kThreads; ++e) {
+            const int idx = e * kThreads + tid;
+            const int kk = idx / kTile;
+            const int ii = idx - kk * kTile;
+            const int k = k0 + kk, i = i0 + ii;
+            const float v = (k < n && i < n) ? __ldg(H + (size_t)k * n + i) : inf;
+            reinterpret_cast<float*>(&Hs[kk >> 1][ii])[kk & 1] = v;
+        }
+        // A slab: rows j0..j0+127, columns k0..k0+15 (coalesced along k)
+#pragma unroll
+        for (int e = 0; e < (kSlab * kTile) / kThreads; ++e) {
+            const int idx = e * kThreads + tid;
+            const int jj = idx / kSlab;
+            const int kk = idx - jj * kSlab;
+            const int k = k0 + kk, j = j0 + jj;
+            const float v = (k < n && j < n) ? __ldg(A + (size_t)j * n + k) : inf;
+            reinterpret_cast<float*>(&As[kk >> 1][jj])[kk & 1] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kp = 0; kp < kSlab / 2; ++kp) {
+            float2 h[8], a[8];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                h[u] = Hs[kp][tx * 4 + u];
+                h[u + 4] = Hs[kp][64 + tx * 4 + u];
+                a[u] = As[kp][ty * 4 + u];
+                a[u + 4] = As[kp][64 + ty * 4 + u];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+#pragma unroll
+                for (int v = 0; v < 8; ++v) {
+                    const float2 s = add2(a[v], h[u]);
+                    acc[u][v] = nsg_min3(acc[u][v], s.x, s.y);
+                }
+        }
+    }
+
+    bool diff = false;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const int i = i0 + (u < 4 ? tx * 4 + u : 64 + tx * 4 + (u - 4));
+        if (i >= n) continue;
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const int j = j0 + (v < 4 ? ty * 4 + v : 64 + ty * 4 + (v - 4));
+            if (j >= n) continue;
+            const size_t o = (size_t)i * n + j;
+            if (__float_as_int(acc[u][v]) != __float_as_int(__ldg(H + o))) diff = true;
+            Hn[o] = acc[u][v];
+        }
+    }
+    if (__syncthreads_or(diff) && tid == 0) changed[step] = 1;
+}
+
+// Back-walk of netcalc/src/hedetniemi_gpu.cu:70-107 over snapshots Hi[p]
+// (H before step p). Diagonal cells hold i.
+__global__ void hedetniemi_walk_kernel(const float* __restrict__ H, const float* __restrict__ Hi,
+                                       const float* __restrict__ A, int* __restrict__ paths,
+                                       float tolerance, int n, int L) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= n || j >= n) return;
+    int* cell = paths + (size_t)i * L * n + (size_t)j * L;
+    if (i == j) {
+        for (int p = 0; p < L; ++p) cell[p] = i;
+        return;
+    }
+    float len = H[(size_t)i * n + j];
+    int k = j;
+    for (int p = L - 1; p >= 0; --p) {
+        const float* hp = Hi + (size_t)p * n * n + (size_t)i * n;
+        for (int q = 0; q < n; ++q) {
+            if (q == j) continue;
+            const float a = A[(size_t)q * n + k];
+            if (__fsub_rn(__fadd_rn(hp[q], a), len) < tolerance) {
+                len = __fsub_rn(len, a);
+                k = q;
+                break;
+            }
+        }
+        cell[p] = k;
+    }
+}
+
+// mode 0: 1/r adjacency (netcalc/src/hedetniemi_gpu.cu:10-26);
+// mode 1: -ln(r) adjacency, evaluated in double and rounded to float.
+__global__ void corr_to_adj_kernel(const float* __restrict__ C, float* __restrict__ A, int n,
+                                   int mode) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)n * n) return;
+    const int i = static_cast<int>(idx / n), j = static_cast<int>(idx % n);
+    const float c = C[idx];
+    const float inf = __int_as_float(0x7f800000);
+    float v;
+    if (i == j) {
+        v = 0.f;
+    } else if (mode == 0) {
+        v = (c == 0.f) ? inf : __fdiv_rn(1.f, c);
+    } else {
+        v = (c > 0.f) ? __double2float_rn(-log(static_cast<double>(c))) : inf;
+    }
+    A[idx] = v;
+}
+
+void launch_step(const float* A, const float* H, float* Hn, int n, int* changed, int step,
+                 cudaStream_t s) {
+    dim3 grid((n + kTile - 1) / kTile, (n + kTile - 1) / kTile);
+    hedetniemi_step_kernel<<<grid, kThreads, 0, s>>>(A, H, Hn, n, changed, step);
+    NSG_CUDA(cudaGetLastError());
+}
+
+struct DevMem {
+    void* p = nullptr;
+    explicit DevMem(size_t bytes) { NSG_CUDA(cudaMalloc(&p, bytes > 0 ? bytes : 1)); }
+    ~DevMem() { if (p) cudaFree(p); }
+    DevMem(const DevMem&) = delete;
+    DevMem& operator=(const DevMem&) = delete;
+};
+
+}  // namespace
+
+int apsp_lengths(const float* A, float* H, int n, int max_path_length, cudaStream_t s) {
+    if (n < 0 || max_path_length < 0) invalid("negative size or path length");
+    const size_t nn = (size_t)n * n;
+    NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    if (max_path_length == 0 || n == 0) return 0;
+    DevMem tmp(nn * sizeof(float));
+    DevMem changed(sizeof(int) * max_path_length);
+    NSG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int) * max_path_length, s));
+    float* buf[2] = {H, static_cast<float*>(tmp.p)};
+    int* ch = static_cast<int*>(changed.p);
+    // Launch in chunks; read the last step's flag between chunks so long runs
+    // stop shortly after the fixed point instead of queueing empty steps.
+    const int chunk = 8;
+    int t = 0;
+    int last_flag = 1;
+    while (t < max_path_length && last_flag) {
+        const int end = std::min(max_path_length, t + chunk);
+        for (; t < end; ++t) launch_step(A, buf[t & 1], buf[(t + 1) & 1], n, ch, t, s);
+        NSG_CUDA(cudaMemcpyAsync(&last_flag, ch + (t - 1), sizeof(int), cudaMemcpyDeviceToHost, s));
+        NSG_CUDA(cudaStreamSynchronize(s));
+    }
+    std::vector<int> flags(t);
+    NSG_CUDA(cudaMemcpyAsync(flags.data(), ch, sizeof(int) * t, cudaMemcpyDeviceToHost, s));
+    NSG_CUDA(cudaStreamSynchronize(s));
+    int steps = t;
+    for (int q = 0; q < t; ++q) {
+        if (flags[q] == 0) {
+            steps = q + 1;
+            break;
+        }
+    }
+    // Result lives in buf[t & 1]; when converged both buffers hold it.
+    if (buf[t & 1] != H) {
+        NSG_CUDA(cudaMemcpyAsync(H, buf[t & 1], nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        NSG_CUDA(cudaStreamSynchronize(s));
+    }
+    return steps;
+}
+
+void apsp_paths(const float* A, float* H, int* paths, int n, int L, float tolerance,
+                cudaStream_t s) {
+    if (n < 0 || L < 1) invalid("paths need n >= 0 and maxPathLength >= 1");
+    const size_t nn = (size_t)n * n;
+    NSG_CUDA(cudaMemsetAsync(paths, 0xff, sizeof(int) * nn * L, s));  // -1
+    if (n == 0) return;
+    DevMem tmp(nn * sizeof(float));
+    DevMem snaps(nn * L * sizeof(float));
+    DevMem changed(sizeof(int) * L);
+    NSG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int) * L, s));
+    NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    float* buf[2] = {H, static_cast<float*>(tmp.p)};
+    float* Hi = static_cast<float*>(snaps.p);
+    for (int p = 0; p < L; ++p) {
+        NSG_CUDA(cudaMemcpyAsync(Hi + nn * p, buf[p & 1], nn * sizeof(float),
+                                 cudaMemcpyDeviceToDevice, s));
+        launch_step(A, buf[p & 1], buf[(p + 1) & 1], n, static_cast<int*>(changed.p), p, s);
+    }
+    if (buf[L & 1] != H) {
+        NSG_CUDA(cudaMemcpyAsync(H, buf[L & 1], nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    dim3 block(32, 8);
+    dim3 grid((n + 31) / 32, (n + 7) / 8);
+    hedetniemi_walk_kernel<<<grid, block, 0, s>>>(H, Hi, A, paths, tolerance, n, L);
+    NSG_CUDA(cudaGetLastError());
+    NSG_CUDA(cudaStreamSynchronize(s));
+}
+
+void corr_to_adjacency(const float* C, float* A, int n, int mode, cudaStream_t s) {
+    if (n <= 0) return;
+    const size_t nn = (size_t)n * n;
+    const int threads = 256;
+    corr_to_adj_kernel<<<static_cast<unsigned>((nn + threads - 1) / threads), threads, 0, s>>>(
+        C, A, n, mode);
+    NSG_CUDA(cudaGetLastError());
+}
+
+}  // namespace nsg

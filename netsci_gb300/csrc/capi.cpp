@@ -1,0 +1,483 @@
+// extern "C" boundary (include/netsci_gb300.h). Every entry point catches
+// C++ exceptions and returns a status; the message stays readable through
+// nsg_last_error() on the calling thread.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <type_traits>
+#include <string>
+#include <vector>
+
+#include "apsp.h"
+#include "cuarray.h"
+#include "engine.h"
+#include "errors.h"
+#include "netcalc/generalized_correlation.h"
+#include "netcalc/hedetniemi.h"
+#include "netcalc/mutual_information.h"
+#include "netcalc/psi.h"
+#include "netsci_gb300.h"
+
+struct nsg_cuarray {
+    int dtype;
+    void* obj;
+};
+
+struct nsg_ksg_plan {
+    nsg::KsgPlan* plan;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        g_last_error.clear();
+        f();
+        return NSG_OK;
+    } catch (const nsg::Error& e) {
+        g_last_error = e.what();
+        return e.status;
+    } catch (const std::invalid_argument& e) {
+        g_last_error = e.what();
+        return std::strcmp(e.what(), "Invalid platform") == 0 ? NSG_ERR_PLATFORM : NSG_ERR_INVALID;
+    } catch (const std::bad_alloc& e) {
+        g_last_error = std::string("host allocation failed: ") + e.what();
+        return NSG_ERR_INVALID;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return NSG_ERR_INVALID;
+    } catch (...) {
+        g_last_error = "unknown error";
+        return NSG_ERR_INVALID;
+    }
+}
+
+template <typename T>
+CuArray<T>* as(nsg_cuarray* a, const char* what) {
+    if (!a || !a->obj) nsg::invalid(std::string(what) + " is null");
+    const int want = std::is_same<T, float>::value ? NSG_DTYPE_FLOAT32
+                     : std::is_same<T, int>::value ? NSG_DTYPE_INT32
+                                                   : NSG_DTYPE_FLOAT64;
+    if (a->dtype != want) nsg::invalid(std::string(what) + " has the wrong element type");
+    return static_cast<CuArray<T>*>(a->obj);
+}
+
+// Dispatch a generic lambda over the handle's element type.
+template <typename F>
+void visit(nsg_cuarray* a, F&& f) {
+    if (!a || !a->obj) nsg::invalid("CuArray handle is null");
+    switch (a->dtype) {
+        case NSG_DTYPE_FLOAT32: f(static_cast<CuArray<float>*>(a->obj)); break;
+        case NSG_DTYPE_INT32: f(static_cast<CuArray<int>*>(a->obj)); break;
+        case NSG_DTYPE_FLOAT64: f(static_cast<CuArray<double>*>(a->obj)); break;
+        default: nsg::invalid("unknown CuArray element type");
+    }
+}
+
+cudaStream_t stream_of(void* s) { return static_cast<cudaStream_t>(s); }
+
+}  // namespace
+
+extern "C" {
+
+const char* nsg_last_error(void) { return g_last_error.c_str(); }
+int nsg_version(void) { return 100; }
+void nsg_free(void* p) { delete[] static_cast<int*>(p); }
+
+// ---- CuArray ---------------------------------------------------------------
+int nsg_cuarray_create(int dtype, nsg_cuarray** out) {
+    return guarded([&] {
+        if (!out) nsg::invalid("out is null");
+        auto* h = new nsg_cuarray{dtype, nullptr};
+        switch (dtype) {
+            case NSG_DTYPE_FLOAT32: h->obj = new CuArray<float>(); break;
+            case NSG_DTYPE_INT32: h->obj = new CuArray<int>(); break;
+            case NSG_DTYPE_FLOAT64: h->obj = new CuArray<double>(); break;
+            default: delete h; nsg::invalid("unknown dtype");
+        }
+        *out = h;
+    });
+}
+
+int nsg_cuarray_destroy(nsg_cuarray* a) {
+    return guarded([&] {
+        if (!a) return;
+        visit(a, [](auto* c) { delete c; });
+        delete a;
+    });
+}
+
+int nsg_cuarray_dtype(const nsg_cuarray* a) { return a ? a->dtype : -1; }
+
+int nsg_cuarray_init(nsg_cuarray* a, int m, int n, int* err) {
+    return guarded([&] { visit(a, [&](auto* c) { *err = c->init(m, n); }); });
+}
+
+int nsg_cuarray_init_from(nsg_cuarray* a, const void* host, int m, int n, int* err) {
+    return guarded([&] {
+        visit(a, [&](auto* c) {
+            using T = std::remove_pointer_t<std::remove_reference_t<decltype(c->host())>>;
+            *err = c->init(const_cast<T*>(static_cast<const T*>(host)), m, n);
+        });
+    });
+}
+
+int nsg_cuarray_from_cuarray_shallow(nsg_cuarray* a, nsg_cuarray* src, int start, int end, int m,
+                                     int n, int* err) {
+    return guarded([&] {
+        if (!src || src->dtype != a->dtype) nsg::invalid("source CuArray type differs");
+        visit(a, [&](auto* c) {
+            *err = c->fromCuArrayShallowCopy(static_cast<decltype(c)>(src->obj), start, end, m, n);
+        });
+    });
+}
+
+int nsg_cuarray_from_cuarray_deep(nsg_cuarray* a, nsg_cuarray* src, int start, int end, int m,
+                                  int n, int* err) {
+    return guarded([&] {
+        if (!src || src->dtype != a->dtype) nsg::invalid("source CuArray type differs");
+        visit(a, [&](auto* c) {
+            *err = c->fromCuArrayDeepCopy(static_cast<decltype(c)>(src->obj), start, end, m, n);
+        });
+    });
+}
+
+int nsg_cuarray_from_host(nsg_cuarray* a, const void* data, int m, int n, int* err) {
+    return nsg_cuarray_init_from(a, data, m, n, err);
+}
+
+int nsg_cuarray_shape(const nsg_cuarray* a, int* m, int* n, int* size, size_t* bytes, int* owner,
+                      int* ah, int* ad) {
+    return guarded([&] {
+        visit(const_cast<nsg_cuarray*>(a), [&](auto* c) {
+            if (m) *m = c->m();
+            if (n) *n = c->n();
+            if (size) *size = c->size();
+            if (bytes) *bytes = c->bytes();
+            if (owner) *owner = c->owner();
+            if (ah) *ah = c->allocatedHost();
+            if (ad) *ad = c->allocatedDevice();
+        });
+    });
+}
+
+void* nsg_cuarray_host(nsg_cuarray* a) {
+    void* p = nullptr;
+    if (guarded([&] { visit(a, [&](auto* c) { p = c->host(); }); }) != NSG_OK) return nullptr;
+    return p;
+}
+
+void* nsg_cuarray_device(nsg_cuarray* a) {
+    void* p = nullptr;
+    if (guarded([&] { visit(a, [&](auto* c) { p = c->device(); }); }) != NSG_OK) return nullptr;
+    return p;
+}
+
+#define NSG_CUARRAY_OP(NAME, CALL)                                             \
+    int NAME(nsg_cuarray* a, int* err) {                                       \
+        return guarded([&] { visit(a, [&](auto* c) { *err = c->CALL(); }); }); \
+    }
+NSG_CUARRAY_OP(nsg_cuarray_allocate_host, allocateHost)
+NSG_CUARRAY_OP(nsg_cuarray_allocate_device, allocateDevice)
+NSG_CUARRAY_OP(nsg_cuarray_to_device, toDevice)
+NSG_CUARRAY_OP(nsg_cuarray_to_host, toHost)
+NSG_CUARRAY_OP(nsg_cuarray_deallocate_host, deallocateHost)
+NSG_CUARRAY_OP(nsg_cuarray_deallocate_device, deallocateDevice)
+#undef NSG_CUARRAY_OP
+
+int nsg_cuarray_get(const nsg_cuarray* a, int i, int j, double* value) {
+    return guarded([&] {
+        visit(const_cast<nsg_cuarray*>(a), [&](auto* c) {
+            if (!c->allocatedHost() || i < 0 || j < 0 || i >= c->m() || j >= c->n()) {
+                nsg::invalid("CuArray index out of range");
+            }
+            *value = static_cast<double>(c->get(i, j));
+        });
+    });
+}
+
+int nsg_cuarray_set(nsg_cuarray* a, double value, int i, int j, int* err) {
+    return guarded([&] {
+        visit(a, [&](auto* c) {
+            using T = std::remove_pointer_t<std::remove_reference_t<decltype(c->host())>>;
+            *err = c->set(static_cast<T>(value), i, j);
+        });
+    });
+}
+
+int nsg_cuarray_load(nsg_cuarray* a, const char* path, int* err) {
+    return guarded([&] {
+        if (!path) nsg::invalid("path is null");
+        visit(a, [&](auto* c) { *err = c->load(path); });
+    });
+}
+
+int nsg_cuarray_save(nsg_cuarray* a, const char* path) {
+    return guarded([&] {
+        if (!path) nsg::invalid("path is null");
+        visit(a, [&](auto* c) { c->save(path); });
+    });
+}
+
+int nsg_cuarray_sort(nsg_cuarray* a, int i, nsg_cuarray** out) {
+    return guarded([&] {
+        visit(a, [&](auto* c) {
+            if (i < 0 || i >= c->m()) nsg::invalid("row index out of range");
+            *out = new nsg_cuarray{a->dtype, c->sort(i)};
+        });
+    });
+}
+
+int nsg_cuarray_argsort(nsg_cuarray* a, int i, nsg_cuarray** out) {
+    return guarded([&] {
+        visit(a, [&](auto* c) {
+            if (i < 0 || i >= c->m()) nsg::invalid("row index out of range");
+            *out = new nsg_cuarray{NSG_DTYPE_INT32, c->argsort(i)};
+        });
+    });
+}
+
+// ---- netcalc ---------------------------------------------------------------
+int nsg_mutual_information(nsg_cuarray* X, nsg_cuarray* I, nsg_cuarray* ab, int k, int n, int xd,
+                           int d, int platform, int* result) {
+    return guarded([&] {
+        *result = netcalc::mutualInformation(as<float>(X, "X"), as<float>(I, "I"),
+                                             as<int>(ab, "ab"), k, n, xd, d, platform);
+    });
+}
+
+int nsg_mutual_information_checkpointed(nsg_cuarray* X, nsg_cuarray* I, nsg_cuarray* ab, int k,
+                                        int n, int xd, int d, int platform, int freq,
+                                        const char* file, int* result) {
+    return guarded([&] {
+        if (!file) nsg::invalid("checkpoint file name is null");
+        *result = netcalc::mutualInformation(as<float>(X, "X"), as<float>(I, "I"),
+                                             as<int>(ab, "ab"), k, n, xd, d, platform, freq, file);
+    });
+}
+
+int nsg_mutual_information_gpu(nsg_cuarray* Xa, nsg_cuarray* Xb, int k, int n, int xd, int d,
+                               float* result) {
+    return guarded([&] {
+        *result = netcalc::mutualInformationGpu(as<float>(Xa, "Xa"), as<float>(Xb, "Xb"), k, n,
+                                                xd, d);
+    });
+}
+
+int nsg_mutual_information_cpu(nsg_cuarray* Xa, nsg_cuarray* Xb, int k, int n, int xd, int d,
+                               float* result) {
+    return guarded([&] {
+        *result = netcalc::mutualInformationCpu(as<float>(Xa, "Xa"), as<float>(Xb, "Xb"), k, n,
+                                                xd, d);
+    });
+}
+
+int nsg_generalized_correlation(nsg_cuarray* X, nsg_cuarray* R, nsg_cuarray* ab, int k, int n,
+                                int xd, int d, int platform, int* result) {
+    return guarded([&] {
+        *result = netcalc::generalizedCorrelation(as<float>(X, "X"), as<float>(R, "R"),
+                                                  as<int>(ab, "ab"), k, n, xd, d, platform);
+    });
+}
+
+int nsg_generalized_correlation_checkpointed(nsg_cuarray* X, nsg_cuarray* R, nsg_cuarray* ab,
+                                             int k, int n, int xd, int d, int platform, int freq,
+                                             const char* file, int* result) {
+    return guarded([&] {
+        if (!file) nsg::invalid("checkpoint file name is null");
+        *result = netcalc::generalizedCorrelation(as<float>(X, "X"), as<float>(R, "R"),
+                                                  as<int>(ab, "ab"), k, n, xd, d, platform, freq,
+                                                  file);
+    });
+}
+
+int nsg_generalized_correlation_gpu(nsg_cuarray* Xa, nsg_cuarray* Xb, int k, int n, int xd,
+                                    int d, float* result) {
+    return guarded([&] {
+        *result = netcalc::generalizedCorrelationGpu(as<float>(Xa, "Xa"), as<float>(Xb, "Xb"), k,
+                                                     n, xd, d);
+    });
+}
+
+int nsg_generalized_correlation_cpu(nsg_cuarray* Xa, nsg_cuarray* Xb, int k, int n, int xd,
+                                    int d, float* result) {
+    return guarded([&] {
+        *result = netcalc::generalizedCorrelationCpu(as<float>(Xa, "Xa"), as<float>(Xb, "Xb"), k,
+                                                     n, xd, d);
+    });
+}
+
+int nsg_generate_restart_ab_from_checkpoint_file(nsg_cuarray* ab, nsg_cuarray* restart,
+                                                 const char* file) {
+    return guarded([&] {
+        if (!file) nsg::invalid("checkpoint file name is null");
+        netcalc::generateRestartAbFromCheckpointFile(as<int>(ab, "ab"), as<int>(restart, "restartAb"),
+                                                     file);
+    });
+}
+
+int nsg_hedetniemi_all_shortest_paths(nsg_cuarray* A, nsg_cuarray* H, nsg_cuarray* paths, int L,
+                                      float tol, int platform) {
+    return guarded([&] {
+        netcalc::hedetniemiAllShortestPaths(as<float>(A, "A"), as<float>(H, "H"),
+                                            as<int>(paths, "paths"), L, tol, platform);
+    });
+}
+
+int nsg_hedetniemi_all_shortest_paths_gpu(nsg_cuarray* A, nsg_cuarray* H, nsg_cuarray* paths,
+                                          float tol, int L) {
+    return guarded([&] {
+        netcalc::hedetniemiAllShortestPathsGpu(as<float>(A, "A"), as<float>(H, "H"),
+                                               as<int>(paths, "paths"), tol, L);
+    });
+}
+
+int nsg_hedetniemi_all_shortest_path_lengths(nsg_cuarray* A, nsg_cuarray* H, int L,
+                                             int platform) {
+    return guarded([&] {
+        netcalc::hedetniemiAllShortestPathLengths(as<float>(A, "A"), as<float>(H, "H"), L,
+                                                  platform);
+    });
+}
+
+int nsg_hedetniemi_all_shortest_path_lengths_gpu(nsg_cuarray* A, nsg_cuarray* H, int L) {
+    return guarded([&] {
+        netcalc::hedetniemiAllShortestPathLengthsGpu(as<float>(A, "A"), as<float>(H, "H"), L);
+    });
+}
+
+int nsg_correlation_to_adjacency(nsg_cuarray* A, nsg_cuarray* C, int n, int platform) {
+    return guarded([&] {
+        netcalc::correlationToAdjacency(as<float>(A, "A"), as<float>(C, "C"), n, platform);
+    });
+}
+
+int nsg_recover_single_shortest_path(nsg_cuarray* paths, int L, int i, int j, int** path,
+                                     int* len) {
+    return guarded([&] {
+        CuArray<int>* p = as<int>(paths, "paths");
+        if (L < 1) nsg::invalid("maxPathLength must be >= 1");
+        const int n = static_cast<int>(std::sqrt(static_cast<double>(p->n() / L)));
+        if (i < 0 || j < 0 || i >= n || j >= n) nsg::invalid("node index out of range");
+        int* dim = nullptr;
+        netcalc::recoverSingleShortestPath(path, &dim, p, L, i, j);
+        *len = dim[0];
+        delete[] dim;
+    });
+}
+
+int nsg_generate_psi(nsg_cuarray* psi, int n) {
+    return guarded([&] { generatePsi(as<float>(psi, "psi"), n); });
+}
+
+// ---- device-pointer entry points ----------------------------------------------
+int nsg_ksg_pairs_device(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi,
+                         float* gc, float* w, void* stream) {
+    return guarded([&] {
+        if (npairs < 0 || (npairs && !pairs)) nsg::invalid("bad pair list");
+        std::vector<nsg_ksg_pair> v(pairs, pairs + npairs);
+        nsg::KsgOutputs o;
+        o.mi = mi;
+        o.gc = gc;
+        o.w = w;
+        nsg::KsgPlan plan(v, k, d, o, nsg::KsgPlanOptions{});
+        plan.run(stream_of(stream));
+        // the plan's descriptors and scratch are released on return
+        NSG_CUDA(cudaStreamSynchronize(stream_of(stream)));
+    });
+}
+
+int nsg_ksg_pair_detail_device(const float* xa, const float* xb, int ld, int m, int k, int d,
+                               int* n_x, int* n_y, float* eps_x, float* eps_y, float* kdist,
+                               float* mi, void* stream) {
+    return guarded([&] {
+        std::vector<nsg_ksg_pair> v{{xa, xb, nullptr, ld, m}};
+        nsg::KsgOutputs o;
+        o.mi = mi;
+        o.nx = n_x;
+        o.ny = n_y;
+        o.eps_x = eps_x;
+        o.eps_y = eps_y;
+        o.kdist = kdist;
+        nsg::KsgPlan plan(v, k, d, o, nsg::KsgPlanOptions{});
+        plan.run(stream_of(stream));
+        NSG_CUDA(cudaStreamSynchronize(stream_of(stream)));
+    });
+}
+
+int nsg_ksg_plan_create(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi, float* gc,
+                        float* w, int flags, nsg_ksg_plan** out) {
+    return guarded([&] {
+        if (!out) nsg::invalid("out is null");
+        if (npairs < 0 || (npairs && !pairs)) nsg::invalid("bad pair list");
+        std::vector<nsg_ksg_pair> v(pairs, pairs + npairs);
+        nsg::KsgOutputs o;
+        o.mi = mi;
+        o.gc = gc;
+        o.w = w;
+        nsg::KsgPlanOptions opt;
+        opt.graph = (flags & 1) != 0;
+        opt.timing = (flags & 2) != 0;
+        *out = new nsg_ksg_plan{new nsg::KsgPlan(v, k, d, o, opt)};
+    });
+}
+
+int nsg_ksg_plan_run(nsg_ksg_plan* plan, void* stream) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        plan->plan->run(stream_of(stream));
+    });
+}
+
+int nsg_ksg_plan_launches(const nsg_ksg_plan* plan, int* launches) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        *launches = plan->plan->launches();
+    });
+}
+
+int nsg_ksg_plan_count_ms(const nsg_ksg_plan* plan, float* ms) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        *ms = plan->plan->count_ms();
+    });
+}
+
+int nsg_ksg_plan_destroy(nsg_ksg_plan* plan) {
+    return guarded([&] {
+        if (!plan) return;
+        delete plan->plan;
+        delete plan;
+    });
+}
+
+int nsg_ksg_set_shape(int threads, int r, int frames, int variant) {
+    return guarded([&] { nsg::ksg_force_shape(threads, r, frames, variant); });
+}
+
+int nsg_apsp_lengths_device(const float* A, float* H, int n, int L, int* steps, void* stream) {
+    return guarded([&] {
+        const int s = nsg::apsp_lengths(A, H, n, L, stream_of(stream));
+        if (steps) *steps = s;
+    });
+}
+
+int nsg_apsp_paths_device(const float* A, float* H, int* paths, int n, int L, float tol,
+                          void* stream) {
+    return guarded([&] { nsg::apsp_paths(A, H, paths, n, L, tol, stream_of(stream)); });
+}
+
+int nsg_corr_to_adjacency_device(const float* C, float* A, int n, int mode, void* stream) {
+    return guarded([&] {
+        if (mode != 0 && mode != 1) nsg::invalid("mode must be 0 (1/r) or 1 (-ln r)");
+        nsg::corr_to_adjacency(C, A, n, mode, stream_of(stream));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+// Shared definitions for the netsci_gb300 CUDA library: status codes, error
+// capture, and the small device helpers the KSG and Hedetniemi kernels share.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "errors.h"
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+
+// Chebyshev helpers. Distances are |x_i - x_j| rounded once (subtract) and
+// then combined with exact max operations, the arithmetic of
+// netcalc/src/mutual_information_cpu.cpp:28-46, so every distance and every
+// comparison is bit-identical to the reference CPU path.
+__device__ __forceinline__ float nsg_absdiff(float a, float b) { return fabsf(a - b); }
+
+// Three-input maximum (sm_100+ PTX form, one instruction).
+__device__ __forceinline__ float nsg_max3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+__device__ __forceinline__ float nsg_min3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Packed pair subtraction: two IEEE round-to-nearest subtractions in one
+// instruction on sm_100+ (sub.rn.f32x2); bit-identical to two scalar FSUBs.
+__device__ __forceinline__ float2 nsg_sub2(float2 a, float2 b) {
+    unsigned long long ra, rb, rr;
+    ra = (static_cast<unsigned long long>(__float_as_uint(a.y)) << 32) | __float_as_uint(a.x);
+    rb = (static_cast<unsigned long long>(__float_as_uint(b.y)) << 32) | __float_as_uint(b.x);
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rr) : "l"(ra), "l"(rb));
+    return make_float2(__uint_as_float(static_cast<unsigned>(rr & 0xffffffffu)),
+                       __uint_as_float(static_cast<unsigned>(rr >> 32)));
+}
+
+// Bounded mbarrier wait (phase parity). Returns false when the iteration
+// limit runs out; callers record FAULT_WAIT_TIMEOUT and leave.
+__device__ __forceinline__ bool nsg_mbar_wait(uint32_t bar_smem, uint32_t parity,
+                                              uint32_t max_iters) {
+    for (uint32_t it = 0; it < max_iters; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar_smem), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t nsg_smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}

@@ -1,0 +1,338 @@
+// KSG planner (see engine.h).
+#include "engine.h"
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+
+#include "errors.h"
+#include "ksg_registry.cuh"
+
+namespace nsg {
+
+// ---------------------------------------------------------------------------
+// DeviceBuffer
+// ---------------------------------------------------------------------------
+DeviceBuffer::DeviceBuffer(size_t bytes) { reset(bytes); }
+DeviceBuffer::~DeviceBuffer() {
+    if (p_) cudaFree(p_);
+}
+DeviceBuffer::DeviceBuffer(DeviceBuffer&& o) noexcept : p_(o.p_), bytes_(o.bytes_) {
+    o.p_ = nullptr;
+    o.bytes_ = 0;
+}
+DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
+    if (this != &o) {
+        if (p_) cudaFree(p_);
+        p_ = o.p_;
+        bytes_ = o.bytes_;
+        o.p_ = nullptr;
+        o.bytes_ = 0;
+    }
+    return *this;
+}
+void DeviceBuffer::reset(size_t bytes) {
+    if (p_) {
+        cudaFree(p_);
+        p_ = nullptr;
+        bytes_ = 0;
+    }
+    if (bytes) {
+        NSG_CUDA(cudaMalloc(&p_, bytes));
+        bytes_ = bytes;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// psi tables
+// ---------------------------------------------------------------------------
+void host_psi(float* psi, int n) {
+    for (int i = 0; i <= n; ++i) psi[i] = 0.0f;
+    if (n >= 1) psi[1] = static_cast<float>(-0.57721566490153);
+    for (int i = 1; i < n; ++i) {
+        const float inv = static_cast<float>(1.0 / static_cast<float>(i));
+        psi[i + 1] = psi[i] + inv;
+    }
+}
+
+namespace {
+std::mutex g_psi_mu;
+struct PsiCache {
+    int device = -1;
+    int n = -1;
+    std::shared_ptr<DeviceBuffer> buf;
+};
+PsiCache g_psi[16];
+
+std::mutex g_shape_mu;
+KsgShape g_forced{0, 0, 0};
+int g_forced_variant = -1;
+}  // namespace
+
+std::shared_ptr<const DeviceBuffer> device_psi(int n) {
+    int dev = 0;
+    NSG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_psi_mu);
+    PsiCache& c = g_psi[dev & 15];
+    if (c.device != dev || c.n < n || !c.buf) {
+        // The recurrence is prefix-stable: a longer table serves every m below it.
+        const int len = std::max(n, std::max(c.device == dev ? c.n : 0, 1024));
+        std::vector<float> h(static_cast<size_t>(len) + 1);
+        host_psi(h.data(), len);
+        auto b = std::make_shared<DeviceBuffer>(h.size() * sizeof(float));
+        NSG_CUDA(cudaMemcpy(b->get(), h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+        c.device = dev;
+        c.n = len;
+        c.buf = b;
+    }
+    return c.buf;
+}
+
+void ksg_force_shape(int threads, int r, int frames, int variant) {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    g_forced = {threads, r, frames};
+    g_forced_variant = variant;
+}
+
+int sm_count() {
+    static int cached[16] = {0};
+    int dev = 0;
+    NSG_CUDA(cudaGetDevice(&dev));
+    if (!cached[dev & 15]) {
+        int v = 0;
+        NSG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        cached[dev & 15] = v;
+    }
+    return cached[dev & 15];
+}
+
+// ---------------------------------------------------------------------------
+// KsgPlan
+// ---------------------------------------------------------------------------
+namespace {
+
+long long count_items(const std::vector<nsg_ksg_pair>& pairs, int qc) {
+    long long c = 0;
+    for (const auto& p : pairs) c += (p.m + qc - 1) / qc;
+    return c;
+}
+
+}  // namespace
+
+KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const KsgOutputs& out,
+                 const KsgPlanOptions& opt)
+    : d_(d), k_(k), kmax_(ksg_kmax_for(k)), timing_(opt.timing), out_(out), graph_(opt.graph) {
+    if (d < 1 || d > 3) invalid("d must be 1, 2 or 3 (got " + std::to_string(d) + ")");
+    if (k < 1) invalid("k must be >= 1");
+    if (kmax_ == 0) fail(NSG_ERR_UNSUPPORTED, "k > 32 is not supported by the GPU path");
+    const int npairs = static_cast<int>(pairs.size());
+    npairs_ = npairs;
+    int maxm = 0;
+    long long total_samples = 0;
+    for (int p = 0; p < npairs; ++p) {
+        const auto& q = pairs[p];
+        if (!q.xa || !q.xb) invalid("pair " + std::to_string(p) + " has a null row pointer");
+        if (q.m < k + 1) {
+            invalid("pair " + std::to_string(p) + ": k must be smaller than the number of samples (k=" +
+                    std::to_string(k) + ", m=" + std::to_string(q.m) + ")");
+        }
+        if (!q.fmap && q.ld < q.m) invalid("pair " + std::to_string(p) + ": ld < m");
+        if (q.ld < 1) invalid("pair " + std::to_string(p) + ": ld < 1");
+        maxm = std::max(maxm, q.m);
+        total_samples += q.m;
+    }
+    const bool per_sample = out.nx || out.ny || out.eps_x || out.eps_y || out.kdist;
+
+    // ---- tile shape -----------------------------------------------------
+    {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        if (g_forced.threads) {
+            shape_ = g_forced;
+            variant_ = g_forced_variant;
+        }
+    }
+    if (shape_.threads) {
+        if (!ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_)) {
+            fail(NSG_ERR_UNSUPPORTED, "forced KSG shape is not instantiated for this d/k");
+        }
+    } else {
+        // Largest per-CTA query block that still gives every resident CTA
+        // slot two work items; otherwise the smallest block.
+        const KsgKernelEntry* cand[32];
+        const int nc = std::min(32, ksg_list_entries(d, kmax_, cand, 32));
+        const int sms = sm_count();
+        const KsgKernelEntry* best = nullptr;
+        long long best_q = -1;
+        const KsgKernelEntry* smallest = nullptr;
+        const KsgShape pref = ksg_default_shape(d, kmax_);
+        for (int i = 0; i < nc; ++i) {
+            const KsgKernelEntry* e = cand[i];
+            if (e->variant != cand[0]->variant) continue;  // default variant family only
+            const long long qc = static_cast<long long>(e->threads) * e->r;
+            if (!smallest || qc < static_cast<long long>(smallest->threads) * smallest->r) smallest = e;
+            const long long slots = static_cast<long long>(sms) * std::max(1, e->ctas_per_sm());
+            if (count_items(pairs, static_cast<int>(qc)) < 2 * slots) continue;
+            const bool is_pref = e->threads == pref.threads && e->r == pref.r && e->frames == pref.frames;
+            if (qc > best_q || (qc == best_q && is_pref)) {
+                best = e;
+                best_q = qc;
+            }
+        }
+        if (!best) best = smallest;
+        if (!best) fail(NSG_ERR_UNSUPPORTED, "no KSG kernel for this d/k");
+        shape_ = {best->threads, best->r, best->frames};
+        variant_ = best->variant;
+    }
+    const KsgKernelEntry* entry = ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_);
+    variant_ = entry->variant;
+    const int qc = shape_.threads * shape_.r;
+
+    // ---- order, batches, descriptors, items ------------------------------
+    std::vector<int> order(npairs);
+    std::iota(order.begin(), order.end(), 0);
+    // longest pairs first (their count kernels take longest)
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return pairs[a].m > pairs[b].m; });
+    std::vector<long long> prefix(npairs + 1, 0);
+    for (int p = 0; p < npairs; ++p) prefix[p + 1] = prefix[p] + pairs[p].m;
+
+    size_t budget = opt.scratch_budget_bytes ? opt.scratch_budget_bytes : (size_t(1) << 31);
+    long long budget_floats = static_cast<long long>(budget / sizeof(float));
+    if (per_sample) budget_floats = std::max<long long>(budget_floats, total_samples);
+
+    std::vector<KsgPairDesc> descs(npairs);
+    std::vector<KsgItem> items;
+    long long scratch_need = 0;
+    int pos = 0;
+    while (pos < npairs) {
+        Batch b;
+        b.pair0 = pos;
+        b.item0 = static_cast<int>(items.size());
+        long long used = 0;
+        while (pos < npairs && (b.npairs == 0 || used + pairs[order[pos]].m <= budget_floats)) {
+            const int src = order[pos];
+            const auto& q = pairs[src];
+            KsgPairDesc& dd = descs[pos];
+            dd.xa = q.xa;
+            dd.xb = q.xb;
+            dd.fmap = q.fmap;
+            dd.ld = q.ld;
+            dd.m = q.m;
+            dd.out = src;
+            dd.pad = 0;
+            dd.scratch = per_sample ? prefix[src] : used;
+            for (int q0 = 0; q0 < q.m; q0 += qc) {
+                items.push_back({pos, q0, std::min(q.m, q0 + qc), 0});
+            }
+            used += q.m;
+            ++b.npairs;
+            ++pos;
+        }
+        b.nitems = static_cast<int>(items.size()) - b.item0;
+        const int slots = sm_count() * std::max(1, entry->ctas_per_sm());
+        b.grid = std::max(1, std::min(b.nitems, slots));
+        scratch_need = std::max(scratch_need, per_sample ? total_samples : used);
+        batches_.push_back(b);
+    }
+
+    if (npairs) {
+        pairs_dev_.reset(descs.size() * sizeof(KsgPairDesc));
+        NSG_CUDA(cudaMemcpy(pairs_dev_.get(), descs.data(), descs.size() * sizeof(KsgPairDesc),
+                            cudaMemcpyHostToDevice));
+        items_dev_.reset(items.size() * sizeof(KsgItem));
+        NSG_CUDA(cudaMemcpy(items_dev_.get(), items.data(), items.size() * sizeof(KsgItem),
+                            cudaMemcpyHostToDevice));
+        scratch_.reset(static_cast<size_t>(scratch_need) * sizeof(float));
+        counters_.reset(batches_.size() * sizeof(int));
+        fault_.reset(sizeof(int));
+        NSG_CUDA(cudaMemset(fault_.get(), 0, sizeof(int)));
+        psi_ = device_psi(maxm);
+    }
+    if (timing_) {
+        events_.resize(2 * batches_.size());
+        for (auto& e : events_) NSG_CUDA(cudaEventCreate(&e));
+    }
+}
+
+KsgPlan::~KsgPlan() {
+    for (auto e : events_) cudaEventDestroy(e);
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (capture_stream_) cudaStreamDestroy(capture_stream_);
+}
+
+void KsgPlan::enqueue(cudaStream_t s) {
+    if (batches_.empty()) return;
+    NSG_CUDA(cudaMemsetAsync(counters_.get(), 0, batches_.size() * sizeof(int), s));
+    for (size_t bi = 0; bi < batches_.size(); ++bi) {
+        const Batch& b = batches_[bi];
+        KsgCountArgs a{};
+        a.pairs = pairs_dev_.as<KsgPairDesc>();
+        a.items = items_dev_.as<KsgItem>() + b.item0;
+        a.nitems = b.nitems;
+        a.k = k_;
+        a.counter = counters_.as<int>() + bi;
+        a.fault = fault_.as<int>();
+        a.psi = psi_->as<float>();
+        a.psum = scratch_.as<float>();
+        a.nx = out_.nx;
+        a.ny = out_.ny;
+        a.eps_x = out_.eps_x;
+        a.eps_y = out_.eps_y;
+        a.kdist = out_.kdist;
+        if (timing_) NSG_CUDA(cudaEventRecord(events_[2 * bi], s));
+        ksg_launch_counts(a, d_, kmax_, shape_, b.grid, s);
+        if (timing_) NSG_CUDA(cudaEventRecord(events_[2 * bi + 1], s));
+        KsgFinalArgs f{};
+        f.pairs = pairs_dev_.as<KsgPairDesc>() + b.pair0;
+        f.npairs = b.npairs;
+        f.k = k_;
+        f.d = d_;
+        f.psi = psi_->as<float>();
+        f.psum = scratch_.as<float>();
+        f.mi = out_.mi;
+        f.gc = out_.gc;
+        f.w = out_.w;
+        ksg_launch_final(f, s);
+    }
+}
+
+float KsgPlan::count_ms() const {
+    if (!timing_) fail(NSG_ERR_INVALID, "plan was created without timing events");
+    float total = 0.f;
+    for (size_t b = 0; b < batches_.size(); ++b) {
+        NSG_CUDA(cudaEventSynchronize(events_[2 * b + 1]));
+        float ms = 0.f;
+        NSG_CUDA(cudaEventElapsedTime(&ms, events_[2 * b], events_[2 * b + 1]));
+        total += ms;
+    }
+    return total;
+}
+
+void KsgPlan::run(cudaStream_t s) {
+    if (!graph_) {
+        enqueue(s);
+        return;
+    }
+    if (!exec_) {
+        NSG_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
+        NSG_CUDA(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
+        try {
+            enqueue(capture_stream_);
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(capture_stream_, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        cudaGraph_t g = nullptr;
+        NSG_CUDA(cudaStreamEndCapture(capture_stream_, &g));
+        const cudaError_t e = cudaGraphInstantiate(&exec_, g, 0);
+        cudaGraphDestroy(g);
+        NSG_CUDA(e);
+    }
+    NSG_CUDA(cudaGraphLaunch(exec_, s));
+}
+
+}  // namespace nsg

@@ -1,0 +1,102 @@
+// Host-side KSG planner: turns a list of variable pairs into device
+// descriptors, a work queue and scratch, and runs it as one persistent
+// count launch plus one finalize launch per batch (optionally captured in a
+// CUDA graph).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "ksg.cuh"
+#include "netsci_gb300.h"
+
+namespace nsg {
+
+// Device allocation owned by the library.
+class DeviceBuffer {
+public:
+    DeviceBuffer() = default;
+    explicit DeviceBuffer(size_t bytes);
+    ~DeviceBuffer();
+    DeviceBuffer(DeviceBuffer&& o) noexcept;
+    DeviceBuffer& operator=(DeviceBuffer&& o) noexcept;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    void* get() const { return p_; }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p_); }
+    size_t bytes() const { return bytes_; }
+    void reset(size_t bytes);
+
+private:
+    void* p_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+struct KsgOutputs {
+    float* mi = nullptr;     // device, indexed by pair order of the input list
+    float* gc = nullptr;
+    float* w = nullptr;
+    // optional per-sample outputs (device, length = total samples over pairs,
+    // pair p's samples at the prefix offset of p in input order)
+    int* nx = nullptr;
+    int* ny = nullptr;
+    float* eps_x = nullptr;
+    float* eps_y = nullptr;
+    float* kdist = nullptr;
+};
+
+struct KsgPlanOptions {
+    bool graph = false;                  // capture each run in a CUDA graph
+    bool timing = false;                 // CUDA events around each count launch
+    size_t scratch_budget_bytes = 0;     // 0: library default
+};
+
+class KsgPlan {
+public:
+    KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const KsgOutputs& out,
+            const KsgPlanOptions& opt);
+    ~KsgPlan();
+    void run(cudaStream_t s);
+    int launches() const { return 2 * static_cast<int>(batches_.size()); }
+    // Device time of the count kernels of the last run (ms); needs timing.
+    float count_ms() const;
+    long long pairs() const { return npairs_; }
+    const KsgShape& shape() const { return shape_; }
+    int variant() const { return variant_; }
+
+private:
+    struct Batch {
+        int pair0 = 0, npairs = 0;
+        int item0 = 0, nitems = 0;
+        int grid = 0;
+    };
+    void enqueue(cudaStream_t s);
+
+    int d_, k_, kmax_;
+    long long npairs_ = 0;
+    bool timing_ = false;
+    std::vector<cudaEvent_t> events_;
+    KsgShape shape_{};
+    int variant_ = -1;
+    KsgOutputs out_;
+    std::vector<Batch> batches_;
+    DeviceBuffer pairs_dev_, items_dev_, scratch_, counters_, fault_;
+    std::shared_ptr<const DeviceBuffer> psi_;
+    bool graph_ = false;
+    cudaGraphExec_t exec_ = nullptr;
+    cudaStream_t capture_stream_ = nullptr;
+};
+
+// Device psi table with at least n+1 entries (shared, grown on demand).
+std::shared_ptr<const DeviceBuffer> device_psi(int n);
+// Host psi table of the reference recurrence (netcalc/src/psi.cpp:6-20).
+void host_psi(float* psi, int n);
+
+// Shape override set by nsg_ksg_set_shape (threads == 0: automatic).
+void ksg_force_shape(int threads, int r, int frames, int variant);
+int sm_count();
+
+}  // namespace nsg

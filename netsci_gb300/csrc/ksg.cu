@@ -1,0 +1,122 @@
+// KSG finalize kernel and kernel-registry lookups.
+#include <cmath>
+
+#include "common.cuh"
+#include "ksg.cuh"
+#include "ksg_registry.cuh"
+
+namespace nsg {
+namespace {
+
+// One thread per pair: the float sum of the pair's per-sample psi terms in
+// sample order, then the KSG formula and the generalized-correlation
+// transform, with the reference's operation order and precisions:
+//   netcalc/src/mutual_information_gpu.cu:1065-1074 (sum, divide, formula)
+//   netcalc/src/generalized_correlation_gpu.cpp:16-31 (transform in double)
+// The sum is sequential on purpose: it reproduces the reference's float
+// rounding sequence exactly, and costs about m dependent adds per pair.
+__global__ void ksg_final_kernel(KsgFinalArgs A) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= A.npairs) return;
+    const KsgPairDesc P = A.pairs[p];
+    const int m = P.m;
+    const float* __restrict__ s = A.psum + P.scratch;
+    float avg = 0.f;
+    for (int q = 0; q < m; ++q) avg = __fadd_rn(avg, __ldg(s + q));
+    avg = __fdiv_rn(avg, static_cast<float>(m));
+    const float inv_k = __double2float_rn(__ddiv_rn(1.0, static_cast<double>(static_cast<float>(A.k))));
+    const float mi = __fsub_rn(__fsub_rn(__fadd_rn(__ldg(A.psi + m), __ldg(A.psi + A.k)), inv_k), avg);
+    if (A.mi) A.mi[P.out] = mi;
+    if (A.gc || A.w) {
+        float gc = 0.f;
+        if (static_cast<double>(mi) > 0.0) {
+            const double scale = -(2.0 / static_cast<double>(static_cast<float>(A.d)));
+            const float e = __double2float_rn(exp(scale * static_cast<double>(mi)));
+            gc = __double2float_rn(sqrt(1.0 - static_cast<double>(e)));
+        }
+        if (A.gc) A.gc[P.out] = gc;
+        if (A.w) {
+            A.w[P.out] = gc > 0.f ? __double2float_rn(-log(static_cast<double>(gc)))
+                                  : __int_as_float(0x7f800000);
+        }
+    }
+}
+
+}  // namespace
+
+int ksg_kmax_for(int k) {
+    if (k < 1) return 0;
+    if (k <= 4) return 4;
+    if (k <= 8) return 8;
+    if (k <= 16) return 16;
+    if (k <= 32) return 32;
+    return 0;
+}
+
+static const KsgKernelEntry* entries_for(int d, int* count) {
+    switch (d) {
+        case 1: return ksg_entries_d1(count);
+        case 2: return ksg_entries_d2(count);
+        case 3: return ksg_entries_d3(count);
+        default: *count = 0; return nullptr;
+    }
+}
+
+const KsgKernelEntry* ksg_find_entry(int d, int kmax, int threads, int r, int frames,
+                                     int variant) {
+    int n = 0;
+    const KsgKernelEntry* e = entries_for(d, &n);
+    for (int i = 0; i < n; ++i) {
+        if (e[i].kmax == kmax && e[i].threads == threads && e[i].r == r &&
+            e[i].frames == frames && (variant < 0 || e[i].variant == variant)) {
+            return &e[i];
+        }
+    }
+    return nullptr;
+}
+
+int ksg_list_entries(int d, int kmax, const KsgKernelEntry** out, int cap) {
+    int n = 0, c = 0;
+    const KsgKernelEntry* e = entries_for(d, &n);
+    for (int i = 0; i < n; ++i) {
+        if (e[i].kmax == kmax) {
+            if (c < cap) out[c] = &e[i];
+            ++c;
+        }
+    }
+    return c;
+}
+
+KsgShape ksg_default_shape(int d, int kmax) {
+    (void)d;
+    if (kmax >= 32) return {128, 1, 1024};
+    if (kmax >= 16) return {128, 2, 1024};
+    return {128, 2, 1024};
+}
+
+bool ksg_shape_supported(int d, int kmax, const KsgShape& s) {
+    return ksg_find_entry(d, kmax, s.threads, s.r, s.frames, -1) != nullptr;
+}
+
+int ksg_ctas_per_sm(int d, int kmax, const KsgShape& s) {
+    const KsgKernelEntry* e = ksg_find_entry(d, kmax, s.threads, s.r, s.frames, -1);
+    return e ? e->ctas_per_sm() : 0;
+}
+
+void ksg_launch_counts(const KsgCountArgs& a, int d, int kmax, const KsgShape& s, int grid,
+                       cudaStream_t st) {
+    const KsgKernelEntry* e = ksg_find_entry(d, kmax, s.threads, s.r, s.frames, -1);
+    if (!e) fail(NSG_ERR_UNSUPPORTED, "no KSG kernel instantiated for this shape");
+    e->launch(a, grid, st);
+    NSG_CUDA(cudaGetLastError());
+}
+
+void ksg_launch_final(const KsgFinalArgs& a, cudaStream_t st) {
+    if (a.npairs <= 0) return;
+    const int threads = 128;
+    const int grid = (a.npairs + threads - 1) / threads;
+    ksg_final_kernel<<<grid, threads, 0, st>>>(a);
+    NSG_CUDA(cudaGetLastError());
+}
+
+}  // namespace nsg

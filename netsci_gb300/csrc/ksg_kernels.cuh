@@ -1,0 +1,306 @@
+// KSG mutual-information count kernel (templated body; instantiated per
+// dimension in ksg_d1.cu, ksg_d2.cu, ksg_d3.cu so the builds run in parallel).
+//
+// What one CTA does for a work item (pair p, query samples q0..q1):
+//
+//   * Each thread owns R query samples i (strided by the CTA size so that
+//     neighbouring threads own neighbouring samples) and keeps their 2d
+//     coordinates in registers.
+//   * Pass 1 streams every frame j of the pair through a shared-memory tile
+//     (structure-of-arrays: one row of `frames` floats per coordinate plane),
+//     reads frames four at a time as float4 broadcasts, and forms the joint
+//     Chebyshev distance dz = max(d_a, d_b). A per-sample sorted list of the
+//     KMAX smallest (dz, j) lives in registers; it is only touched when the
+//     minimum dz of the four frames does not exceed the current k-th entry,
+//     which after the first few hundred frames is rare.
+//   * eps_a / eps_b are the largest marginal distances over the k list
+//     entries (netcalc/src/mutual_information_cpu.cpp:54-77).
+//   * Pass 2 streams the frames again and counts d_a <= eps_a and
+//     d_b <= eps_b over all j (self included, then minus one,
+//     netcalc/src/mutual_information_cpu.cpp:78-109).
+//   * The sample's psi[n_x] + psi[n_y] (float add, :110) goes to the pair's
+//     scratch row; ksg_final_kernel sums the row in sample order.
+//
+// Runtime k <= KMAX: the first KMAX-k list slots hold (-inf, -1) sentinels that
+// no candidate can displace, so the live k-list occupies the last k slots and
+// the admission threshold is always slot KMAX-1 (a static register index).
+//
+// Tie rule: candidates are ordered by (dz, j). The reference's std::sort
+// leaves equal distances unordered; the two agree on tie-free inputs and on
+// ties between frames with equal marginals (exact duplicates).
+//
+// Arithmetic: one rounded subtraction per coordinate, then exact abs/max, and
+// exact compares, so distances, eps and counts are bit-identical to the
+// reference CPU path.
+#pragma once
+
+#include "common.cuh"
+#include "ksg.cuh"
+
+namespace nsg {
+namespace ksgk {
+
+__device__ __forceinline__ bool lex_less(float v, int j, float bv, int bj) {
+    return v < bv || (v == bv && j < bj);
+}
+
+// Insert (v, j) into the ascending list (bd, bj); the caller has checked
+// that (v, j) sorts before the last entry. Branch-free over the slots.
+template <int KMAX>
+__device__ __forceinline__ void topk_insert(float (&bd)[KMAX], int (&bj)[KMAX], float v, int j) {
+#pragma unroll
+    for (int s = KMAX - 1; s >= 0; --s) {
+        const int p = s > 0 ? s - 1 : 0;
+        const bool lt_prev = (s > 0) && lex_less(v, j, bd[p], bj[p]);
+        const bool lt_cur = lex_less(v, j, bd[s], bj[s]);
+        const float nd = lt_prev ? bd[p] : (lt_cur ? v : bd[s]);
+        const int nj = lt_prev ? bj[p] : (lt_cur ? j : bj[s]);
+        bd[s] = nd;
+        bj[s] = nj;
+    }
+}
+
+// Variant 0: scalar subtractions, two-input max chain.
+// Variant 1: packed f32x2 subtractions (two frames per instruction) and the
+//            three-input max.
+// Variant 2: packed f32x2 subtractions, two-input max chain.
+template <int D, int VARIANT>
+struct Marg {
+    // Marginal Chebyshev distances of the four frames of a group (frames in
+    // the x,y,z,w lanes of g[c]) from the query coordinates q[c].
+    __device__ __forceinline__ static void four(const float (&q)[D], const float4 (&g)[D],
+                                                float (&out)[4]) {
+        if constexpr (VARIANT == 0) {
+            float a[4] = {fabsf(q[0] - g[0].x), fabsf(q[0] - g[0].y), fabsf(q[0] - g[0].z),
+                          fabsf(q[0] - g[0].w)};
+#pragma unroll
+            for (int c = 1; c < D; ++c) {
+                a[0] = fmaxf(a[0], fabsf(q[c] - g[c].x));
+                a[1] = fmaxf(a[1], fabsf(q[c] - g[c].y));
+                a[2] = fmaxf(a[2], fabsf(q[c] - g[c].z));
+                a[3] = fmaxf(a[3], fabsf(q[c] - g[c].w));
+            }
+#pragma unroll
+            for (int f = 0; f < 4; ++f) out[f] = a[f];
+        } else {
+            float lo[D][4];
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const float2 u = nsg_sub2(make_float2(q[c], q[c]), make_float2(g[c].x, g[c].y));
+                const float2 v = nsg_sub2(make_float2(q[c], q[c]), make_float2(g[c].z, g[c].w));
+                lo[c][0] = fabsf(u.x);
+                lo[c][1] = fabsf(u.y);
+                lo[c][2] = fabsf(v.x);
+                lo[c][3] = fabsf(v.y);
+            }
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                if constexpr (D == 1) {
+                    out[f] = lo[0][f];
+                } else if constexpr (D == 2) {
+                    out[f] = fmaxf(lo[0][f], lo[1][f]);
+                } else {
+                    if constexpr (VARIANT == 1) {
+                        out[f] = nsg_max3(lo[0][f], lo[1][f], lo[2][f]);
+                    } else {
+                        out[f] = fmaxf(fmaxf(lo[0][f], lo[1][f]), lo[2][f]);
+                    }
+                }
+            }
+        }
+    }
+};
+
+template <int D>
+__device__ __forceinline__ float marginal_at(const float (&q)[D], const float* __restrict__ x,
+                                             int ld, int src) {
+    float v = fabsf(q[0] - __ldg(x + src));
+#pragma unroll
+    for (int c = 1; c < D; ++c) v = fmaxf(v, fabsf(q[c] - __ldg(x + (size_t)c * ld + src)));
+    return v;
+}
+
+template <int D, int KMAX, int R, int NT, int J, int VARIANT>
+__global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
+    static_assert(J % (4 * 32) == 0, "tile must hold whole float4 groups");
+    __shared__ __align__(16) float tile[2 * D][J];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    const float kInf = __int_as_float(0x7f800000);
+
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(A.counter, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= A.nitems) return;
+        const KsgItem w = A.items[item];
+        const KsgPairDesc P = A.pairs[w.pair];
+        const int m = P.m;
+        const int ld = P.ld;
+        const int* __restrict__ fmap = P.fmap;
+        const float* __restrict__ xa = P.xa;
+        const float* __restrict__ xb = P.xb;
+
+        // query samples of this thread
+        float qa[R][D], qb[R][D];
+        int qi[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            qi[r] = w.q0 + r * NT + tid;
+            const bool valid = qi[r] < w.q1;
+            const int src = valid ? (fmap ? __ldg(fmap + qi[r]) : qi[r]) : 0;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                qa[r][c] = valid ? __ldg(xa + (size_t)c * ld + src) : 0.f;
+                qb[r][c] = valid ? __ldg(xb + (size_t)c * ld + src) : 0.f;
+            }
+        }
+
+        float bd[R][KMAX];
+        int bj[R][KMAX];
+        const int nsent = KMAX - A.k;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int s = 0; s < KMAX; ++s) {
+                bd[r][s] = s < nsent ? -kInf : kInf;
+                bj[r][s] = s < nsent ? -1 : 0x7fffffff;
+            }
+
+        const int ntiles = (m + J - 1) / J;
+
+        // ---- pass 1: k nearest joint neighbours ------------------------------
+        for (int t = 0; t < ntiles; ++t) {
+            const int j0 = t * J;
+            __syncthreads();
+            for (int idx = tid; idx < 2 * D * J; idx += NT) {
+                const int c = idx / J;
+                const int f = idx - c * J;
+                const int j = j0 + f;
+                float v = kInf;
+                if (j < m) {
+                    const int src = fmap ? __ldg(fmap + j) : j;
+                    v = c < D ? __ldg(xa + (size_t)c * ld + src)
+                              : __ldg(xb + (size_t)(c - D) * ld + src);
+                }
+                tile[c][f] = v;
+            }
+            __syncthreads();
+            const int jn = min(J, m - j0);
+            const int ngroups = (jn + 3) >> 2;
+            for (int g = 0; g < ngroups; ++g) {
+                float4 ga[D], gb[D];
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    ga[c] = *reinterpret_cast<const float4*>(&tile[c][4 * g]);
+                    gb[c] = *reinterpret_cast<const float4*>(&tile[D + c][4 * g]);
+                }
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    float da[4], db[4], dz[4];
+                    Marg<D, VARIANT>::four(qa[r], ga, da);
+                    Marg<D, VARIANT>::four(qb[r], gb, db);
+#pragma unroll
+                    for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
+                    const float mn = fminf(fminf(dz[0], dz[1]), fminf(dz[2], dz[3]));
+                    if (mn <= bd[r][KMAX - 1]) {
+#pragma unroll
+                        for (int f = 0; f < 4; ++f) {
+                            const int j = j0 + 4 * g + f;
+                            if (j < m && j != qi[r] &&
+                                lex_less(dz[f], j, bd[r][KMAX - 1], bj[r][KMAX - 1])) {
+                                topk_insert<KMAX>(bd[r], bj[r], dz[f], j);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+
+        // ---- eps from the k neighbours ---------------------------------------
+        float ea[R], eb[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            ea[r] = 0.f;
+            eb[r] = 0.f;
+            const bool valid = qi[r] < w.q1;
+#pragma unroll
+            for (int s = 0; s < KMAX; ++s) {
+                const int j = bj[r][s];
+                if (valid && j >= 0 && j < m) {
+                    const int src = fmap ? __ldg(fmap + j) : j;
+                    ea[r] = fmaxf(ea[r], marginal_at<D>(qa[r], xa, ld, src));
+                    eb[r] = fmaxf(eb[r], marginal_at<D>(qb[r], xb, ld, src));
+                }
+            }
+        }
+
+        // ---- pass 2: marginal counts ------------------------------------------
+        int ca[R], cb[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            ca[r] = 0;
+            cb[r] = 0;
+        }
+        for (int t = 0; t < ntiles; ++t) {
+            const int j0 = t * J;
+            if (ntiles > 1) {
+                __syncthreads();
+                for (int idx = tid; idx < 2 * D * J; idx += NT) {
+                    const int c = idx / J;
+                    const int f = idx - c * J;
+                    const int j = j0 + f;
+                    float v = kInf;
+                    if (j < m) {
+                        const int src = fmap ? __ldg(fmap + j) : j;
+                        v = c < D ? __ldg(xa + (size_t)c * ld + src)
+                                  : __ldg(xb + (size_t)(c - D) * ld + src);
+                    }
+                    tile[c][f] = v;
+                }
+                __syncthreads();
+            }
+            const int jn = min(J, m - j0);
+            const int ngroups = (jn + 3) >> 2;
+            for (int g = 0; g < ngroups; ++g) {
+                float4 ga[D], gb[D];
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    ga[c] = *reinterpret_cast<const float4*>(&tile[c][4 * g]);
+                    gb[c] = *reinterpret_cast<const float4*>(&tile[D + c][4 * g]);
+                }
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    float da[4], db[4];
+                    Marg<D, VARIANT>::four(qa[r], ga, da);
+                    Marg<D, VARIANT>::four(qb[r], gb, db);
+#pragma unroll
+                    for (int f = 0; f < 4; ++f) {
+                        ca[r] += da[f] <= ea[r] ? 1 : 0;
+                        cb[r] += db[f] <= eb[r] ? 1 : 0;
+                    }
+                }
+            }
+        }
+
+        // ---- per-sample outputs -----------------------------------------------
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (qi[r] < w.q1) {
+                const long long o = P.scratch + qi[r];
+                const int nx = ca[r] - 1;
+                const int ny = cb[r] - 1;
+                A.psum[o] = __fadd_rn(__ldg(A.psi + nx), __ldg(A.psi + ny));
+                if (A.nx) A.nx[o] = nx;
+                if (A.ny) A.ny[o] = ny;
+                if (A.eps_x) A.eps_x[o] = ea[r];
+                if (A.eps_y) A.eps_y[o] = eb[r];
+                if (A.kdist) A.kdist[o] = bd[r][KMAX - 1];
+            }
+        }
+    }
+}
+
+}  // namespace ksgk
+}  // namespace nsg

@@ -1,0 +1,277 @@
+"""KSG mutual information / generalized correlation on the GPU against the
+CPU oracle and the reference's golden values.
+
+Bar: MI bit-exact (the kernels reproduce the reference's distances, counts
+and float summation order), per-sample n_x / n_y / eps bit-exact, GC
+bit-exact through the CuArray API (host transform, as the reference) and
+within 1e-6 absolute through the device transform.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN_MI = {1000: 0.8449974060058594, 2000: 0.8485465049743652}
+
+
+def _dev_pair(xa, xb, d, m):
+    """(d, ld) device rows for one pair."""
+    from netsci_gb300 import device
+    X, mm = device.pack_trajectory(np.stack([xa, xb]).reshape(2, d * m), d)
+    assert mm == m
+    return X
+
+
+def _mi_device(xa, xb, m, k, d):
+    from netsci_gb300 import device
+    X = _dev_pair(xa, xb, d, m)
+    return device.ksg_pair_detail(X[0], X[1], m, k, d)
+
+
+@pytest.mark.parametrize("n", [1000, 2000])
+def test_gaussian_goldens_gpu_equals_cpu(golden, n):
+    import cuarray
+    import netcalc
+    g = golden("gaussian")
+    xa, xb = cuarray.FloatCuArray(), cuarray.FloatCuArray()
+    xa.fromNumpy1D(g[f"x{n}"])
+    xb.fromNumpy1D(g[f"y{n}"])
+    gpu = netcalc.mutualInformationGpu(Xa=xa, Xb=xb, k=4, n=n, xd=2, d=1)
+    cpu = netcalc.mutualInformationCpu(Xa=xa, Xb=xb, k=4, n=n, xd=2, d=1)
+    assert gpu == cpu == GOLDEN_MI[n]
+
+
+@pytest.mark.parametrize("n", [1000, 2000])
+def test_per_sample_counts_match_oracle(golden, n):
+    g = golden("gaussian")
+    out = _mi_device(g[f"x{n}"], g[f"y{n}"], n, 4, 1)
+    for key in ("n_x", "n_y", "eps_x", "eps_y", "kdist"):
+        got = out[key].cpu().numpy()
+        assert np.array_equal(got, g[f"{key}{n}"]), key
+    assert float(out["mi"].item()) == GOLDEN_MI[n]
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+@pytest.mark.parametrize("n", [1000, 2000])
+def test_reference_curves(golden, d, n):
+    import cuarray
+    import netcalc
+    c = golden("curves")
+    xa, xb = cuarray.FloatCuArray(), cuarray.FloatCuArray()
+    xa.fromNumpy1D(c[f"xa_d{d}_n{n}"])
+    xb.fromNumpy1D(c[f"xb_d{d}_n{n}"])
+    mi = netcalc.mutualInformationGpu(Xa=xa, Xb=xb, k=4, n=n, xd=2, d=d)
+    assert mi == float(c[f"mi_d{d}_n{n}"]) == netcalc.mutualInformationCpu(
+        Xa=xa, Xb=xb, k=4, n=n, xd=2, d=d)
+    gc = netcalc.generalizedCorrelationGpu(Xa=xa, Xb=xb, k=4, n=n, xd=2, d=d)
+    assert gc == float(c[f"gc_d{d}_n{n}"]) == netcalc.generalizedCorrelationCpu(
+        Xa=xa, Xb=xb, k=4, n=n, xd=2, d=d)
+
+
+def test_random_cases_bit_exact(golden):
+    r = golden("random")
+    for i in range(int(r["count"])):
+        d, k, n = (int(v) for v in r[f"meta{i}"])
+        out = _mi_device(r[f"xa{i}"], r[f"xb{i}"], n, k, d)
+        assert float(out["mi"].item()) == float(r[f"mi{i}"]), (i, d, k, n)
+
+
+def test_per_sample_outputs_random_vs_oracle(oracle_mod):
+    rng = np.random.default_rng(11)
+    for d, k, n in ((1, 3, 777), (2, 6, 1031), (3, 6, 1500), (3, 17, 640), (2, 32, 500)):
+        xa = rng.standard_normal(d * n).astype(np.float32)
+        xb = (0.5 * xa + rng.standard_normal(d * n)).astype(np.float32)
+        mi, det = oracle_mod.mi_pair(xa, xb, n, k, d, detail=True)
+        out = _mi_device(xa, xb, n, k, d)
+        for key in ("n_x", "n_y", "eps_x", "eps_y", "kdist"):
+            assert np.array_equal(out[key].cpu().numpy(), det[key]), (d, k, n, key)
+        assert float(out["mi"].item()) == mi
+
+
+SHAPES = [(128, 2, 1024), (128, 4, 512), (256, 1, 1024), (64, 4, 512), (256, 2, 1024),
+          (64, 1, 512)]
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_every_shape_and_variant_agrees(oracle_mod, variant):
+    from netsci_gb300 import device
+    rng = np.random.default_rng(3)
+    n, k, d = 1500, 6, 3
+    xa = rng.standard_normal(d * n).astype(np.float32)
+    xb = (0.8 * xa + 0.6 * rng.standard_normal(d * n)).astype(np.float32)
+    mi, det = oracle_mod.mi_pair(xa, xb, n, k, d, detail=True)
+    try:
+        for shape in SHAPES:
+            device.set_ksg_shape(*shape, variant=variant)
+            out = _mi_device(xa, xb, n, k, d)
+            assert float(out["mi"].item()) == mi, shape
+            assert np.array_equal(out["n_x"].cpu().numpy(), det["n_x"]), shape
+    finally:
+        device.set_ksg_shape(0)
+
+
+def test_protein56_all_pairs_cuarray_api(golden):
+    import cuarray
+    import netcalc
+    z = golden("protein56")
+    X = cuarray.FloatCuArray()
+    X.fromNumpy2D(z["X"])
+    ab = cuarray.IntCuArray()
+    ab.fromNumpy2D(z["ab"])
+    R = cuarray.FloatCuArray()
+    assert netcalc.generalizedCorrelation(X=X, R=R, ab=ab, k=6, n=1000, xd=2, d=3,
+                                          platform=netcalc.GPU_PLATFORM) == 0
+    assert np.array_equal(R.toNumpy1D(), z["gc"])
+
+
+def test_protein56_device_plan_graph(golden, oracle_mod):
+    from netsci_gb300 import device
+    z = golden("protein56")
+    X, m = device.pack_trajectory(z["X"], 3)
+    pairs = device.make_pairs(X, m, z["ab"])
+    P = len(pairs)
+    mi = torch.empty(P, device="cuda")
+    gc = torch.empty(P, device="cuda")
+    w = torch.empty(P, device="cuda")
+    plan = device.KsgPlan(pairs, 6, 3, mi=mi, gc=gc, w=w, graph=True)
+    plan.run()
+    torch.cuda.synchronize()
+    g1 = gc.cpu().numpy()
+    np.testing.assert_allclose(g1, z["gc"], rtol=0, atol=1e-6)
+    assert (g1 == z["gc"]).mean() > 0.999
+    mis = mi.cpu().numpy()
+    for p in (0, 100, 1539):
+        a, b = z["ab"][p]
+        assert mis[p] == oracle_mod.mi_pair(z["X"][a], z["X"][b], 1000, 6, 3)
+    wv = w.cpu().numpy()
+    ref_w = np.where(g1 > 0, (-np.log(g1.astype(np.float64))).astype(np.float32), np.inf)
+    np.testing.assert_array_max_ulp(wv[np.isfinite(ref_w)], ref_w[np.isfinite(ref_w)], maxulp=1)
+    assert np.all(np.isinf(wv[~np.isfinite(ref_w)]))
+    # replays are deterministic
+    for _ in range(2):
+        gc.zero_()
+        plan.run()
+        torch.cuda.synchronize()
+        assert np.array_equal(gc.cpu().numpy(), g1)
+    assert plan.launches == 2
+
+
+def test_uneven_trajectories_one_plan(oracle_mod):
+    from netsci_gb300 import device, synthetic
+    rng = np.random.default_rng(9)
+    pairs, expect, keep = [], [], []
+    for t in range(4):
+        N = int(rng.integers(4, 8))
+        m = int(rng.integers(150, 700))
+        X, _ = synthetic.protein_trajectory(N, m, seed=100 + t)
+        Xd, mm = device.pack_trajectory(X, 3)
+        keep.append(Xd)
+        ab = synthetic.all_pairs(N)
+        pairs += device.make_pairs(Xd, mm, ab)
+        expect += list(oracle_mod.pairs(X, m, 3, ab, 6, gc=False, threads=8))
+    mi = torch.empty(len(pairs), device="cuda")
+    device.ksg_pairs(pairs, 6, 3, mi=mi)
+    assert np.array_equal(mi.cpu().numpy(), np.asarray(expect, np.float32))
+
+
+def test_bootstrap_frame_map_matches_resampled_data(oracle_mod):
+    from netsci_gb300 import device, synthetic
+    N, m, k = 6, 400, 6
+    X, _ = synthetic.protein_trajectory(N, m, seed=4)
+    Xd, mm = device.pack_trajectory(X, 3)
+    rng = np.random.default_rng(1)
+    idx = rng.integers(0, m, size=m).astype(np.int32)   # with replacement
+    fmap = torch.from_numpy(idx).cuda()
+    ab = synthetic.all_pairs(N)
+    pairs = device.make_pairs(Xd, mm, ab, fmap=fmap, m_samples=m)
+    mi = torch.empty(len(pairs), device="cuda")
+    device.ksg_pairs(pairs, k, 3, mi=mi)
+    Xr = X.reshape(N, 3, m)[:, :, idx].reshape(N, 3 * m)
+    expect = oracle_mod.pairs(Xr, m, 3, ab, k, gc=False, threads=8)
+    assert np.array_equal(mi.cpu().numpy(), expect)
+
+
+def test_edge_sizes_and_duplicates(oracle_mod):
+    rng = np.random.default_rng(21)
+    for d, k, n in ((1, 1, 2), (2, 1, 3), (3, 4, 5), (1, 6, 7), (3, 6, 33), (2, 32, 33),
+                    (3, 31, 1029)):
+        xa = rng.standard_normal(d * n).astype(np.float32)
+        xb = rng.standard_normal(d * n).astype(np.float32)
+        mi = oracle_mod.mi_pair(xa, xb, n, k, d)
+        assert float(_mi_device(xa, xb, n, k, d)["mi"].item()) == mi, (d, k, n)
+    # exact duplicate frames (ties with equal marginals are benign)
+    n, d, k = 300, 3, 4
+    base = rng.standard_normal((d, n // 3)).astype(np.float32)
+    xa = np.concatenate([base, base, base], axis=1).ravel()
+    xb = np.concatenate([base * 2, base * 2, base * 2], axis=1).ravel().astype(np.float32)
+    mi = oracle_mod.mi_pair(xa, xb, n, k, d)
+    assert float(_mi_device(xa, xb, n, k, d)["mi"].item()) == mi
+
+
+def test_invalid_k_statuses():
+    from netsci_gb300 import NsgError, device
+    xa = np.random.default_rng(0).standard_normal(100).astype(np.float32)
+    X = _dev_pair(xa, xa, 1, 100)
+    with pytest.raises(NsgError) as e:
+        device.ksg_pair_detail(X[0], X[1], 100, 33, 1)
+    assert e.value.status == 4  # k > 32 unsupported on the GPU
+    with pytest.raises(NsgError) as e:
+        device.ksg_pair_detail(X[0], X[1], 100, 100, 1)
+    assert e.value.status == 1  # k >= m
+
+
+def test_large_pair_properties():
+    """m = 10000 (the large configuration's frame count): symmetry in the
+    pair order and run-to-run determinism."""
+    from netsci_gb300 import device, synthetic
+    X, _ = synthetic.protein_trajectory(3, 10000, seed=77)
+    Xd, m = device.pack_trajectory(X, 3)
+    pairs = device.make_pairs(Xd, m, [[0, 1], [1, 0], [0, 2], [2, 0], [0, 1]])
+    mi = torch.empty(5, device="cuda")
+    device.ksg_pairs(pairs, 6, 3, mi=mi)
+    v = mi.cpu().numpy()
+    assert v[0] == v[1] == v[4] and v[2] == v[3]
+
+
+def test_large_pair_against_oracle_m4000(oracle_mod):
+    from netsci_gb300 import synthetic
+    X, _ = synthetic.protein_trajectory(2, 4000, seed=78)
+    mi = oracle_mod.mi_pair(X[0], X[1], 4000, 6, 3)
+    assert float(_mi_device(X[0], X[1], 4000, 6, 3)["mi"].item()) == mi
+
+
+def test_platform_contract_gpu():
+    import cuarray
+    import netcalc
+    n = 1000
+    x = np.linspace(0.001, np.pi, n).astype(np.float32)
+    X = cuarray.FloatCuArray()
+    X.fromNumpy2D(np.stack([np.sin(x), np.cos(x)]).astype(np.float32))
+    I = cuarray.FloatCuArray()
+    ab = cuarray.IntCuArray()
+    ab.fromNumpy2D(np.array([[0, 1]], np.int32))
+    assert netcalc.mutualInformation(X=X, I=I, ab=ab, k=4, n=n, xd=2, d=1,
+                                     platform=netcalc.GPU_PLATFORM) == 0
+    I2 = cuarray.FloatCuArray()
+    assert netcalc.mutualInformation(X=X, I=I2, ab=ab, k=4, n=n, xd=2, d=1,
+                                     platform=netcalc.CPU_PLATFORM) == 1
+    assert I.get(0, 0) == I2.get(0, 0)
+
+
+def test_checkpointed_gpu_matches_plain(tmp_path):
+    import cuarray
+    import netcalc
+    from netsci_gb300 import synthetic
+    X0, _ = synthetic.protein_trajectory(6, 300, seed=8)
+    X = cuarray.FloatCuArray()
+    X.fromNumpy2D(X0)
+    ab = cuarray.IntCuArray()
+    ab.fromNumpy2D(synthetic.all_pairs(6))
+    R1, R2 = cuarray.FloatCuArray(), cuarray.FloatCuArray()
+    netcalc.generalizedCorrelation(X=X, R=R1, ab=ab, k=6, n=300, xd=2, d=3, platform=0)
+    netcalc.generalizedCorrelationWithCheckpointing(
+        X=X, R=R2, ab=ab, k=6, n=300, xd=2, d=3, platform=0, checkpointFrequency=4,
+        checkpointFileName=str(tmp_path / "run.npy"))
+    assert np.array_equal(R1.toNumpy1D(), R2.toNumpy1D())
+    assert sorted(p.name for p in tmp_path.iterdir()) == ["run_12.npy", "run_ab.npy"]
