@@ -390,6 +390,7 @@ int nsg_ksg_pairs_device(const nsg_ksg_pair* pairs, int npairs, int k, int d, fl
         plan.run(stream_of(stream));
         // the plan's descriptors and scratch are released on return
         NSG_CUDA(cudaStreamSynchronize(stream_of(stream)));
+        if (plan.take_fault()) nsg::fail(NSG_ERR_DEVICE_FAULT, "a frame map entry is outside [0, ld)");
     });
 }
 

@@ -298,6 +298,14 @@ void KsgPlan::enqueue(cudaStream_t s) {
     }
 }
 
+int KsgPlan::take_fault() {
+    if (!fault_.get()) return FAULT_NONE;
+    int f = 0;
+    NSG_CUDA(cudaMemcpy(&f, fault_.get(), sizeof(int), cudaMemcpyDeviceToHost));
+    if (f) NSG_CUDA(cudaMemset(fault_.get(), 0, sizeof(int)));
+    return f;
+}
+
 float KsgPlan::count_ms() const {
     if (!timing_) fail(NSG_ERR_INVALID, "plan was created without timing events");
     float total = 0.f;

@@ -64,6 +64,8 @@ public:
     // Device time of the count kernels of the last run (ms); needs timing.
     float count_ms() const;
     long long pairs() const { return npairs_; }
+    // Reads (and clears) the device fault word; synchronizes with the device.
+    int take_fault();
     const KsgShape& shape() const { return shape_; }
     int variant() const { return variant_; }
 

@@ -111,6 +111,18 @@ struct Marg {
     }
 };
 
+// Source frame of sample s: fmap[s] when a frame map is given. A map entry
+// outside [0, ld) is recorded in the fault word and read as frame 0.
+__device__ __forceinline__ int frame_of(const int* __restrict__ fmap, int s, int ld, int* fault) {
+    if (!fmap) return s;
+    const int f = __ldg(fmap + s);
+    if (f < 0 || f >= ld) {
+        atomicExch(fault, FAULT_BAD_INDEX);
+        return 0;
+    }
+    return f;
+}
+
 template <int D>
 __device__ __forceinline__ float marginal_at(const float (&q)[D], const float* __restrict__ x,
                                              int ld, int src) {
@@ -149,7 +161,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
         for (int r = 0; r < R; ++r) {
             qi[r] = w.q0 + r * NT + tid;
             const bool valid = qi[r] < w.q1;
-            const int src = valid ? (fmap ? __ldg(fmap + qi[r]) : qi[r]) : 0;
+            const int src = valid ? frame_of(fmap, qi[r], ld, A.fault) : 0;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 qa[r][c] = valid ? __ldg(xa + (size_t)c * ld + src) : 0.f;
@@ -180,7 +192,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
                 const int j = j0 + f;
                 float v = kInf;
                 if (j < m) {
-                    const int src = fmap ? __ldg(fmap + j) : j;
+                    const int src = frame_of(fmap, j, ld, A.fault);
                     v = c < D ? __ldg(xa + (size_t)c * ld + src)
                               : __ldg(xb + (size_t)(c - D) * ld + src);
                 }
@@ -229,7 +241,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
             for (int s = 0; s < KMAX; ++s) {
                 const int j = bj[r][s];
                 if (valid && j >= 0 && j < m) {
-                    const int src = fmap ? __ldg(fmap + j) : j;
+                    const int src = frame_of(fmap, j, ld, A.fault);
                     ea[r] = fmaxf(ea[r], marginal_at<D>(qa[r], xa, ld, src));
                     eb[r] = fmaxf(eb[r], marginal_at<D>(qb[r], xb, ld, src));
                 }
@@ -253,7 +265,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
                     const int j = j0 + f;
                     float v = kInf;
                     if (j < m) {
-                        const int src = fmap ? __ldg(fmap + j) : j;
+                        const int src = frame_of(fmap, j, ld, A.fault);
                         v = c < D ? __ldg(xa + (size_t)c * ld + src)
                                   : __ldg(xb + (size_t)(c - D) * ld + src);
                     }
@@ -289,8 +301,10 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
         for (int r = 0; r < R; ++r) {
             if (qi[r] < w.q1) {
                 const long long o = P.scratch + qi[r];
-                const int nx = ca[r] - 1;
-                const int ny = cb[r] - 1;
+                // counts lie in [k, m-1] for finite inputs; the clamp keeps
+                // non-finite inputs from indexing outside the psi table
+                const int nx = min(max(ca[r] - 1, 0), m);
+                const int ny = min(max(cb[r] - 1, 0), m);
                 A.psum[o] = __fadd_rn(__ldg(A.psi + nx), __ldg(A.psi + ny));
                 if (A.nx) A.nx[o] = nx;
                 if (A.ny) A.ny[o] = ny;
