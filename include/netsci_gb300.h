@@ -182,7 +182,10 @@ typedef struct nsg_ksg_plan nsg_ksg_plan;
 int nsg_ksg_plan_create(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi,
                         float* gc, float* w, int flags, nsg_ksg_plan** out);
 int nsg_ksg_plan_run(nsg_ksg_plan* plan, void* stream);
-/* Kernel launches one run makes (count + finalize per batch). */
+/* Raises NSG_ERR_DEVICE_FAULT when the runs so far recorded a device fault
+ * (frame map entry out of range, tie list overflow); synchronizes.        */
+int nsg_ksg_plan_check(nsg_ksg_plan* plan);
+/* Kernel launches one run makes (count, tie resolution, finalize per batch). */
 int nsg_ksg_plan_launches(const nsg_ksg_plan* plan, int* launches);
 /* Device milliseconds of the count kernels in the last run (flag bit 1);
  * waits for that run's events.                                          */

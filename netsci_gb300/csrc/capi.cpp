@@ -390,7 +390,7 @@ int nsg_ksg_pairs_device(const nsg_ksg_pair* pairs, int npairs, int k, int d, fl
         plan.run(stream_of(stream));
         // the plan's descriptors and scratch are released on return
         NSG_CUDA(cudaStreamSynchronize(stream_of(stream)));
-        if (plan.take_fault()) nsg::fail(NSG_ERR_DEVICE_FAULT, "a frame map entry is outside [0, ld)");
+        nsg::raise_fault(plan.take_fault());
     });
 }
 
@@ -409,6 +409,7 @@ int nsg_ksg_pair_detail_device(const float* xa, const float* xb, int ld, int m, 
         nsg::KsgPlan plan(v, k, d, o, nsg::KsgPlanOptions{});
         plan.run(stream_of(stream));
         NSG_CUDA(cudaStreamSynchronize(stream_of(stream)));
+        nsg::raise_fault(plan.take_fault());
     });
 }
 
@@ -433,6 +434,13 @@ int nsg_ksg_plan_run(nsg_ksg_plan* plan, void* stream) {
     return guarded([&] {
         if (!plan || !plan->plan) nsg::invalid("plan is null");
         plan->plan->run(stream_of(stream));
+    });
+}
+
+int nsg_ksg_plan_check(nsg_ksg_plan* plan) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        nsg::raise_fault(plan->plan->take_fault());
     });
 }
 

@@ -126,7 +126,6 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
     : d_(d), k_(k), kmax_(ksg_kmax_for(k)), timing_(opt.timing), out_(out), graph_(opt.graph) {
     if (d < 1 || d > 3) invalid("d must be 1, 2 or 3 (got " + std::to_string(d) + ")");
     if (k < 1) invalid("k must be >= 1");
-    if (kmax_ == 0) fail(NSG_ERR_UNSUPPORTED, "k > 32 is not supported by the GPU path");
     const int npairs = static_cast<int>(pairs.size());
     npairs_ = npairs;
     int maxm = 0;
@@ -143,6 +142,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         maxm = std::max(maxm, q.m);
         total_samples += q.m;
     }
+    if (kmax_ == 0) fail(NSG_ERR_UNSUPPORTED, "k > 32 is not supported by the GPU path");
     const bool per_sample = out.nx || out.ny || out.eps_x || out.eps_y || out.kdist;
 
     // ---- tile shape -----------------------------------------------------
@@ -245,7 +245,22 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         NSG_CUDA(cudaMemcpy(items_dev_.get(), items.data(), items.size() * sizeof(KsgItem),
                             cudaMemcpyHostToDevice));
         scratch_.reset(static_cast<size_t>(scratch_need) * sizeof(float));
-        counters_.reset(batches_.size() * sizeof(int));
+        // per batch: work-queue head, tie count, tie-kernel work counter
+        counters_.reset(3 * batches_.size() * sizeof(int));
+        // Tied samples are rare (about 1e-4 of samples on trajectory data);
+        // the list holds 1/16 of the largest batch's samples.
+        long long batch_samples = 0;
+        for (const Batch& b : batches_) {
+            long long sum = 0;
+            for (int p = b.pair0; p < b.pair0 + b.npairs; ++p) sum += descs[p].m;
+            batch_samples = std::max(batch_samples, sum);
+        }
+        tie_cap_ = static_cast<int>(std::min<long long>(
+            std::max<long long>(65536, batch_samples / 16), 1LL << 30));
+        ties_.reset(static_cast<size_t>(tie_cap_) * sizeof(KsgTie));
+        tie_stride_ = maxm;
+        tie_dz_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(float));
+        tie_idx_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(int));
         fault_.reset(sizeof(int));
         NSG_CUDA(cudaMemset(fault_.get(), 0, sizeof(int)));
         psi_ = device_psi(maxm);
@@ -264,16 +279,20 @@ KsgPlan::~KsgPlan() {
 
 void KsgPlan::enqueue(cudaStream_t s) {
     if (batches_.empty()) return;
-    NSG_CUDA(cudaMemsetAsync(counters_.get(), 0, batches_.size() * sizeof(int), s));
+    NSG_CUDA(cudaMemsetAsync(counters_.get(), 0, 3 * batches_.size() * sizeof(int), s));
     for (size_t bi = 0; bi < batches_.size(); ++bi) {
         const Batch& b = batches_[bi];
+        int* ctr = counters_.as<int>() + 3 * bi;
         KsgCountArgs a{};
         a.pairs = pairs_dev_.as<KsgPairDesc>();
         a.items = items_dev_.as<KsgItem>() + b.item0;
         a.nitems = b.nitems;
         a.k = k_;
-        a.counter = counters_.as<int>() + bi;
+        a.counter = ctr;
         a.fault = fault_.as<int>();
+        a.ties = ties_.as<KsgTie>();
+        a.tie_count = ctr + 1;
+        a.tie_cap = tie_cap_;
         a.psi = psi_->as<float>();
         a.psum = scratch_.as<float>();
         a.nx = out_.nx;
@@ -281,9 +300,30 @@ void KsgPlan::enqueue(cudaStream_t s) {
         a.eps_x = out_.eps_x;
         a.eps_y = out_.eps_y;
         a.kdist = out_.kdist;
-        if (timing_) NSG_CUDA(cudaEventRecord(events_[2 * bi], s));
+        // External records stay real event nodes when the stream is captured.
+        if (timing_) NSG_CUDA(cudaEventRecordWithFlags(events_[2 * bi], s, cudaEventRecordExternal));
         ksg_launch_counts(a, d_, kmax_, shape_, b.grid, s);
-        if (timing_) NSG_CUDA(cudaEventRecord(events_[2 * bi + 1], s));
+        if (timing_) {
+            NSG_CUDA(cudaEventRecordWithFlags(events_[2 * bi + 1], s, cudaEventRecordExternal));
+        }
+        KsgTieArgs t{};
+        t.pairs = pairs_dev_.as<KsgPairDesc>();
+        t.ties = ties_.as<KsgTie>();
+        t.tie_count = ctr + 1;
+        t.tie_cap = tie_cap_;
+        t.tie_next = ctr + 2;
+        t.k = k_;
+        t.fault = fault_.as<int>();
+        t.psi = psi_->as<float>();
+        t.psum = scratch_.as<float>();
+        t.nx = out_.nx;
+        t.ny = out_.ny;
+        t.eps_x = out_.eps_x;
+        t.eps_y = out_.eps_y;
+        t.dz = tie_dz_.as<float>();
+        t.idx = tie_idx_.as<int>();
+        t.stride = tie_stride_;
+        ksg_launch_ties(t, d_, s);
         KsgFinalArgs f{};
         f.pairs = pairs_dev_.as<KsgPairDesc>() + b.pair0;
         f.npairs = b.npairs;

@@ -60,7 +60,8 @@ public:
             const KsgPlanOptions& opt);
     ~KsgPlan();
     void run(cudaStream_t s);
-    int launches() const { return 2 * static_cast<int>(batches_.size()); }
+    // Kernel launches per run: count, tie resolution and finalize per batch.
+    int launches() const { return 3 * static_cast<int>(batches_.size()); }
     // Device time of the count kernels of the last run (ms); needs timing.
     float count_ms() const;
     long long pairs() const { return npairs_; }
@@ -86,6 +87,9 @@ private:
     KsgOutputs out_;
     std::vector<Batch> batches_;
     DeviceBuffer pairs_dev_, items_dev_, scratch_, counters_, fault_;
+    DeviceBuffer ties_, tie_dz_, tie_idx_;
+    int tie_cap_ = 0;
+    long long tie_stride_ = 0;
     std::shared_ptr<const DeviceBuffer> psi_;
     bool graph_ = false;
     cudaGraphExec_t exec_ = nullptr;

@@ -44,12 +44,13 @@ __global__ void ksg_final_kernel(KsgFinalArgs A) {
 
 }  // namespace
 
+// Smallest instantiated list length holding the k+1 nearest neighbours.
 int ksg_kmax_for(int k) {
     if (k < 1) return 0;
-    if (k <= 4) return 4;
-    if (k <= 8) return 8;
-    if (k <= 16) return 16;
-    if (k <= 32) return 32;
+    if (k + 1 <= 6) return 6;
+    if (k + 1 <= 8) return 8;
+    if (k + 1 <= 16) return 16;
+    if (k + 1 <= 32) return 32;
     return 0;
 }
 

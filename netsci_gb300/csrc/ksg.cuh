@@ -32,6 +32,12 @@ struct KsgItem {
     int pad;
 };
 
+// A sample whose k-th and (k+1)-th nearest joint distances are equal.
+struct KsgTie {
+    int pair;             // index into the pair descriptor array
+    int q;                // sample
+};
+
 struct KsgCountArgs {
     const KsgPairDesc* pairs;
     const KsgItem* items;
@@ -39,6 +45,9 @@ struct KsgCountArgs {
     int k;
     int* counter;         // work-queue head, zero before launch
     int* fault;           // device fault word
+    KsgTie* ties;         // tied samples, appended at tie_count
+    int* tie_count;       // zero before launch
+    int tie_cap;
     const float* psi;     // psi table, at least max(m)+1 entries
     float* psum;          // psi[n_x]+psi[n_y] per sample, at pair.scratch + q
     // optional per-sample outputs (null when unused), at pair.scratch + q
@@ -47,6 +56,25 @@ struct KsgCountArgs {
     float* eps_x;
     float* eps_y;
     float* kdist;
+};
+
+struct KsgTieArgs {
+    const KsgPairDesc* pairs;
+    const KsgTie* ties;
+    const int* tie_count;
+    int tie_cap;
+    int* tie_next;        // work counter over tie entries, zero before launch
+    int k;
+    int* fault;
+    const float* psi;
+    float* psum;
+    int* nx;
+    int* ny;
+    float* eps_x;
+    float* eps_y;
+    float* dz;            // per-warp scratch rows of `stride` floats
+    int* idx;             // per-warp scratch rows of `stride` ints
+    long long stride;
 };
 
 struct KsgFinalArgs {
@@ -75,6 +103,9 @@ int ksg_ctas_per_sm(int d, int kmax, const KsgShape& s);
 void ksg_launch_counts(const KsgCountArgs& a, int d, int kmax, const KsgShape& s, int grid,
                        cudaStream_t st);
 void ksg_launch_final(const KsgFinalArgs& a, cudaStream_t st);
+// Warps the tie kernel runs with (scratch rows needed).
+int ksg_tie_warps();
+void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st);
 bool ksg_shape_supported(int d, int kmax, const KsgShape& s);
 
 }  // namespace nsg

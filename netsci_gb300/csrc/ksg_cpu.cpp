@@ -3,12 +3,15 @@
 // falls back to it.
 //
 // Same estimator and arithmetic as netcalc/src/mutual_information_cpu.cpp:
-// 6-121 (joint Chebyshev distances, k nearest by (distance, index), eps as
-// the largest marginal distance over them, marginal counts minus one, float
-// psi sum in sample order). The per-sample work selects the k+1 smallest
-// joint distances instead of sorting all n, and samples are spread over host
-// threads; the per-sample terms are summed afterwards in sample order, so
-// the result is the same float as a sequential pass.
+// 6-121 (joint Chebyshev distances, the k nearest, eps as the largest
+// marginal distance over them, marginal counts minus one, float psi sum in
+// sample order). The per-sample work selects the k+2 smallest joint
+// distances instead of sorting all n; only when the k-th and (k+1)-th are
+// equal (and non-zero), where the neighbour set depends on the order the
+// reference's std::sort leaves equal distances in, is the full index array
+// sorted with the reference's comparator. Samples are spread over host
+// threads and their terms summed afterwards in sample order, so the result
+// is the same float as the reference's sequential pass.
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -36,8 +39,13 @@ void samples_range(const float* xa, const float* xb, int n, int k, int d, const 
         for (int j = 0; j < n; ++j) dz[j] = std::max(marg(xa, n, d, i, j), marg(xb, n, d, i, j));
         std::iota(idx.begin(), idx.end(), 0);
         auto less = [&](int a, int b) { return dz[a] < dz[b] || (dz[a] == dz[b] && a < b); };
-        std::nth_element(idx.begin(), idx.begin() + k, idx.end(), less);
-        std::sort(idx.begin(), idx.begin() + k + 1, less);
+        const int sel = std::min(n, k + 2);
+        std::nth_element(idx.begin(), idx.begin() + (sel - 1), idx.end(), less);
+        std::sort(idx.begin(), idx.begin() + sel, less);
+        if (k + 1 < n && dz[idx[k]] == dz[idx[k + 1]] && dz[idx[k]] > 0.f) {
+            std::iota(idx.begin(), idx.end(), 0);
+            std::sort(idx.begin(), idx.end(), [&](int a, int b) { return dz[a] < dz[b]; });
+        }
         float ex = 0.f, ey = 0.f;
         for (int q = 1; q <= k; ++q) {
             ex = std::max(ex, marg(xa, n, d, i, idx[q]));

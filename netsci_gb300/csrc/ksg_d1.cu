@@ -10,7 +10,7 @@
 namespace nsg {
 namespace {
 const KsgKernelEntry kEntries[] = {
-    NSG_KSG_FAMILY_SMALLK(1, 4, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_SMALLK(1, 6, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_SMALLK(1, 8, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K16(1, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K32(1, NSG_KSG_VARIANT),

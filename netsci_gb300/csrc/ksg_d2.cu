@@ -10,7 +10,7 @@
 namespace nsg {
 namespace {
 const KsgKernelEntry kEntries[] = {
-    NSG_KSG_FAMILY_SMALLK(2, 4, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_SMALLK(2, 6, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_SMALLK(2, 8, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K16(2, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K32(2, NSG_KSG_VARIANT),

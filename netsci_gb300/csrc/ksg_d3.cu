@@ -10,7 +10,7 @@
 namespace nsg {
 namespace {
 const KsgKernelEntry kEntries[] = {
-    NSG_KSG_FAMILY_SMALLK(3, 4, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_SMALLK(3, 6, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_SMALLK(3, 8, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K16(3, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K32(3, NSG_KSG_VARIANT),

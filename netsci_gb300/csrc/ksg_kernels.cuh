@@ -21,13 +21,16 @@
 //   * The sample's psi[n_x] + psi[n_y] (float add, :110) goes to the pair's
 //     scratch row; ksg_final_kernel sums the row in sample order.
 //
-// Runtime k <= KMAX: the first KMAX-k list slots hold (-inf, -1) sentinels that
-// no candidate can displace, so the live k-list occupies the last k slots and
-// the admission threshold is always slot KMAX-1 (a static register index).
+// Runtime k < KMAX: the list keeps the k+1 nearest; its first KMAX-k-1 slots
+// hold (-inf, -1) sentinels that no candidate can displace, so the live
+// entries occupy the last k+1 slots and the admission threshold is always
+// slot KMAX-1 (a static register index).
 //
-// Tie rule: candidates are ordered by (dz, j). The reference's std::sort
-// leaves equal distances unordered; the two agree on tie-free inputs and on
-// ties between frames with equal marginals (exact duplicates).
+// Ties: candidates are ordered by (dz, j). That decides the neighbour set
+// exactly as the reference does whenever the k-th and (k+1)-th distances
+// differ (or are both zero: exact duplicates, whose marginals are zero).
+// Samples where they are equal are handed to ksg_tie_kernel, which replays
+// the reference sort's order for them.
 //
 // Arithmetic: one rounded subtraction per coordinate, then exact abs/max, and
 // exact compares, so distances, eps and counts are bit-identical to the
@@ -117,7 +120,7 @@ __device__ __forceinline__ int frame_of(const int* __restrict__ fmap, int s, int
     if (!fmap) return s;
     const int f = __ldg(fmap + s);
     if (f < 0 || f >= ld) {
-        atomicExch(fault, FAULT_BAD_INDEX);
+        atomicOr(fault, FAULT_BAD_INDEX);
         return 0;
     }
     return f;
@@ -169,9 +172,11 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
             }
         }
 
+        // k+1 live entries: the k nearest plus the next one, so that a tie
+        // between the k-th and (k+1)-th distance is visible.
         float bd[R][KMAX];
         int bj[R][KMAX];
-        const int nsent = KMAX - A.k;
+        const int nsent = KMAX - (A.k + 1);
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -231,14 +236,26 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
         }
 
         // ---- eps from the k neighbours ---------------------------------------
+        // Slots nsent..KMAX-2 hold the k nearest. When the k-th distance
+        // equals the (k+1)-th (and is not zero) the reference's choice among
+        // the equal frames depends on its sort; such samples go to the tie
+        // list and ksg_tie_kernel recomputes them.
         float ea[R], eb[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             ea[r] = 0.f;
             eb[r] = 0.f;
             const bool valid = qi[r] < w.q1;
+            if (valid && bd[r][KMAX - 2] == bd[r][KMAX - 1] && bd[r][KMAX - 2] > 0.f) {
+                const int slot = atomicAdd(A.tie_count, 1);
+                if (slot < A.tie_cap) {
+                    A.ties[slot] = KsgTie{w.pair, qi[r]};
+                } else {
+                    atomicOr(A.fault, FAULT_TIE_OVERFLOW);
+                }
+            }
 #pragma unroll
-            for (int s = 0; s < KMAX; ++s) {
+            for (int s = 0; s < KMAX - 1; ++s) {
                 const int j = bj[r][s];
                 if (valid && j >= 0 && j < m) {
                     const int src = frame_of(fmap, j, ld, A.fault);
@@ -310,7 +327,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
                 if (A.ny) A.ny[o] = ny;
                 if (A.eps_x) A.eps_x[o] = ea[r];
                 if (A.eps_y) A.eps_y[o] = eb[r];
-                if (A.kdist) A.kdist[o] = bd[r][KMAX - 1];
+                if (A.kdist) A.kdist[o] = bd[r][KMAX - 2];
             }
         }
     }

@@ -1,0 +1,152 @@
+// Tie resolution for the KSG count kernel.
+//
+// A sample whose k-th and (k+1)-th nearest joint distances are equal (and
+// non-zero) has a neighbour set that the reference CPU path picks by the
+// order its std::sort leaves equal distances in
+// (netcalc/src/mutual_information_cpu.cpp:48-77). The count kernel appends
+// such samples to a list; this kernel takes them one warp at a time:
+//
+//   1. the warp writes the sample's full joint-distance row (the reference's
+//      arithmetic) and the identity index array into its scratch rows;
+//   2. lane 0 replays the reference sort's order on the prefix that holds
+//      the neighbours (sort_prefix.h);
+//   3. the lanes holding sorted positions 1..k compute eps_a / eps_b, a warp
+//      max-reduction combines them;
+//   4. the marginal counts are recounted over all frames with warp ballots
+//      and population counts, and the sample's psi term is rewritten.
+//
+// Runs between the count kernel and the finalize kernel, with a fixed grid
+// that walks the tie list through an atomic counter (an empty list costs one
+// launch that returns at once).
+#include "common.cuh"
+#include "engine.h"
+#include "ksg.cuh"
+#include "sort_prefix.h"
+
+namespace nsg {
+namespace {
+
+constexpr int kWarpsPerCta = 8;
+constexpr int kCtasPerSm = 2;
+constexpr int kStack = 64;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int tie_frame(const int* __restrict__ fmap, int s, int ld, int* fault) {
+    if (!fmap) return s;
+    const int f = __ldg(fmap + s);
+    if (f < 0 || f >= ld) {
+        atomicOr(fault, FAULT_BAD_INDEX);
+        return 0;
+    }
+    return f;
+}
+
+template <int D>
+__device__ __forceinline__ float tie_marginal(const float (&q)[D], const float* __restrict__ x,
+                                              int ld, int src) {
+    float v = fabsf(q[0] - __ldg(x + src));
+#pragma unroll
+    for (int c = 1; c < D; ++c) v = fmaxf(v, fabsf(q[c] - __ldg(x + (size_t)c * ld + src)));
+    return v;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) ksg_tie_kernel(KsgTieArgs A) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    float* dz = A.dz + warp * A.stride;
+    int* idx = A.idx + warp * A.stride;
+    const int total = min(*A.tie_count, A.tie_cap);
+    for (;;) {
+        int e = 0;
+        if (lane == 0) e = atomicAdd(A.tie_next, 1);
+        e = __shfl_sync(kFull, e, 0);
+        if (e >= total) return;
+        const KsgTie t = A.ties[e];
+        const KsgPairDesc P = A.pairs[t.pair];
+        const int m = P.m, ld = P.ld;
+        const int* __restrict__ fmap = P.fmap;
+        const float* __restrict__ xa = P.xa;
+        const float* __restrict__ xb = P.xb;
+        if (P.m > A.stride) {  // the planner sizes rows for every pair
+            if (lane == 0) atomicOr(A.fault, FAULT_BAD_INDEX);
+            continue;
+        }
+        const int sq = tie_frame(fmap, t.q, ld, A.fault);
+        float qa[D], qb[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            qa[c] = __ldg(xa + (size_t)c * ld + sq);
+            qb[c] = __ldg(xb + (size_t)c * ld + sq);
+        }
+        for (int j = lane; j < m; j += 32) {
+            const int s = tie_frame(fmap, j, ld, A.fault);
+            dz[j] = fmaxf(tie_marginal<D>(qa, xa, ld, s), tie_marginal<D>(qb, xb, ld, s));
+            idx[j] = j;
+        }
+        __syncwarp();
+        int ok = 1;
+        if (lane == 0) {
+            SortSegment stack[kStack];
+            ok = sort_prefix_like_reference(dz, idx, m, A.k + 1, stack, kStack) ? 1 : 0;
+        }
+        ok = __shfl_sync(kFull, ok, 0);
+        __syncwarp();
+        if (!ok) {
+            if (lane == 0) atomicOr(A.fault, FAULT_TIE_UNRESOLVED);
+            continue;
+        }
+        float ea = 0.f, eb = 0.f;
+        if (lane >= 1 && lane <= A.k) {
+            const int s = tie_frame(fmap, idx[lane], ld, A.fault);
+            ea = tie_marginal<D>(qa, xa, ld, s);
+            eb = tie_marginal<D>(qb, xb, ld, s);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            ea = fmaxf(ea, __shfl_xor_sync(kFull, ea, off));
+            eb = fmaxf(eb, __shfl_xor_sync(kFull, eb, off));
+        }
+        int ca = 0, cb = 0;
+        for (int j0 = 0; j0 < m; j0 += 32) {
+            const int j = j0 + lane;
+            bool pa = false, pb = false;
+            if (j < m) {
+                const int s = tie_frame(fmap, j, ld, A.fault);
+                pa = tie_marginal<D>(qa, xa, ld, s) <= ea;
+                pb = tie_marginal<D>(qb, xb, ld, s) <= eb;
+            }
+            ca += __popc(__ballot_sync(kFull, pa));
+            cb += __popc(__ballot_sync(kFull, pb));
+        }
+        if (lane == 0) {
+            const long long o = P.scratch + t.q;
+            const int nx = min(max(ca - 1, 0), m);
+            const int ny = min(max(cb - 1, 0), m);
+            A.psum[o] = __fadd_rn(__ldg(A.psi + nx), __ldg(A.psi + ny));
+            if (A.nx) A.nx[o] = nx;
+            if (A.ny) A.ny[o] = ny;
+            if (A.eps_x) A.eps_x[o] = ea;
+            if (A.eps_y) A.eps_y[o] = eb;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+int ksg_tie_warps() { return sm_count() * kCtasPerSm * kWarpsPerCta; }
+
+void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st) {
+    const int grid = sm_count() * kCtasPerSm;
+    const int threads = kWarpsPerCta * 32;
+    switch (d) {
+        case 1: ksg_tie_kernel<1><<<grid, threads, 0, st>>>(a); break;
+        case 2: ksg_tie_kernel<2><<<grid, threads, 0, st>>>(a); break;
+        case 3: ksg_tie_kernel<3><<<grid, threads, 0, st>>>(a); break;
+        default: fail(NSG_ERR_INVALID, "d must be 1, 2 or 3");
+    }
+    NSG_CUDA(cudaGetLastError());
+}
+
+}  // namespace nsg

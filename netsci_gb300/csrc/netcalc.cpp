@@ -86,6 +86,7 @@ void gpu_pair_list(const DeviceBuffer& xd, int ld, int nodes, CuArray<int>* ab, 
     KsgPlan plan(pairs, k, d, o, KsgPlanOptions{});
     plan.run(nullptr);
     NSG_CUDA(cudaMemcpy(out, mi.get(), sizeof(float) * count, cudaMemcpyDeviceToHost));
+    raise_fault(plan.take_fault());
 }
 
 float gpu_single_pair(CuArray<float>* Xa, CuArray<float>* Xb, int k, int n, int d) {
@@ -105,6 +106,7 @@ float gpu_single_pair(CuArray<float>* Xa, CuArray<float>* Xb, int k, int n, int 
     plan.run(nullptr);
     float r = 0.f;
     NSG_CUDA(cudaMemcpy(&r, mi.get(), sizeof(float), cudaMemcpyDeviceToHost));
+    raise_fault(plan.take_fault());
     return r;
 }
 

@@ -73,7 +73,7 @@ def random_geometric_graph(N: int, mean_degree: float, seed: int, integer_weight
     rng = np.random.default_rng(seed)
     pts = rng.random((N, 3))
     # expected degree ~ (N-1) * (4/3) pi r^3 in the unit cube (edge effects ignored)
-    r = (mean_degree / ((N - 1) * 4.0 / 3.0 * np.pi)) ** (1.0 / 3.0)
+    r = (mean_degree / (max(N - 1, 1) * 4.0 / 3.0 * np.pi)) ** (1.0 / 3.0)
     d2 = ((pts[:, None, :] - pts[None, :, :]) ** 2).sum(-1)
     adj = d2 < r * r
     np.fill_diagonal(adj, False)

@@ -11,14 +11,15 @@
 // :37,64) and, where the reference sources are available, against the
 // reference CPU functions compiled unmodified into oracle/_ref.
 //
-// Tie rule. The reference orders candidates with std::sort on the joint
-// distance alone (netcalc/src/mutual_information_cpu.cpp:48-53), which leaves
-// the order of equal distances unspecified. This restatement orders by
-// (joint distance, frame index), the rule the CUDA kernels use. The two agree
-// whenever the (k+1)-th and (k+2)-th smallest joint distances of a sample
-// differ, and also when tied candidates have equal marginals (exact
-// duplicate frames). oracle_mi_pair reports the number of samples whose
-// neighbour set depends on the tie rule.
+// Tie order. The reference orders each sample's candidates with std::sort
+// over the frame indices, comparing joint distances with `<`
+// (netcalc/src/mutual_information_cpu.cpp:48-53); equal distances end up
+// in whatever order that sort leaves them. This restatement makes the same
+// call with the same comparator on the same index array, so its neighbour
+// sets, and therefore its counts and MI, equal the reference's on every
+// input, tied distances included. oracle_mi_pair also reports how many
+// samples have a tie at the k-th neighbour whose marginals differ (samples
+// whose result depends on that order).
 
 #include <algorithm>
 #include <atomic>
@@ -88,12 +89,10 @@ float oracle_mi_pair(const float* xa, const float* xb, int n, int k, int d,
             float db = marginal(xb, n, d, i, j);
             s.dz[j] = std::max(da, db);
         }
-        // ascending order, :48-53 (tie rule: lower frame index first)
+        // ascending order, :48-53 (the reference's comparator)
         std::iota(s.order.begin(), s.order.end(), 0);
         const float* dz = s.dz.data();
-        std::sort(s.order.begin(), s.order.end(), [dz](int a, int b) {
-            return dz[a] < dz[b] || (dz[a] == dz[b] && a < b);
-        });
+        std::sort(s.order.begin(), s.order.end(), [dz](int a, int b) { return dz[a] < dz[b]; });
         // eps over sorted positions 1..k, :54-77
         float ex = 0.0f, ey = 0.0f;
         for (int q = 1; q < k + 1; ++q) {

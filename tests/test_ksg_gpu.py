@@ -139,7 +139,7 @@ def test_protein56_device_plan_graph(golden, oracle_mod):
     torch.cuda.synchronize()
     g1 = gc.cpu().numpy()
     np.testing.assert_allclose(g1, z["gc"], rtol=0, atol=1e-6)
-    assert (g1 == z["gc"]).mean() > 0.999
+    assert (g1 == z["gc"]).mean() > 0.999  # device exp/sqrt may differ in the last bit
     mis = mi.cpu().numpy()
     for p in (0, 100, 1539):
         a, b = z["ab"][p]
@@ -154,7 +154,7 @@ def test_protein56_device_plan_graph(golden, oracle_mod):
         plan.run()
         torch.cuda.synchronize()
         assert np.array_equal(gc.cpu().numpy(), g1)
-    assert plan.launches == 2
+    assert plan.launches == 3
 
 
 def test_uneven_trajectories_one_plan(oracle_mod):
@@ -214,7 +214,7 @@ def test_invalid_k_statuses():
     xa = np.random.default_rng(0).standard_normal(100).astype(np.float32)
     X = _dev_pair(xa, xa, 1, 100)
     with pytest.raises(NsgError) as e:
-        device.ksg_pair_detail(X[0], X[1], 100, 33, 1)
+        device.ksg_pair_detail(X[0], X[1], 100, 40, 1)
     assert e.value.status == 4  # k > 32 unsupported on the GPU
     with pytest.raises(NsgError) as e:
         device.ksg_pair_detail(X[0], X[1], 100, 100, 1)
@@ -275,3 +275,19 @@ def test_checkpointed_gpu_matches_plain(tmp_path):
         checkpointFileName=str(tmp_path / "run.npy"))
     assert np.array_equal(R1.toNumpy1D(), R2.toNumpy1D())
     assert sorted(p.name for p in tmp_path.iterdir()) == ["run_12.npy", "run_ab.npy"]
+
+
+@pytest.mark.parametrize("d,k,n", [(1, 4, 700), (2, 6, 900), (3, 6, 1000), (3, 10, 600)])
+def test_tied_samples_follow_reference_sort_order(oracle_mod, d, k, n):
+    """Coordinates on a coarse grid make many samples' k-th and (k+1)-th
+    joint distances equal; the GPU must then pick the neighbours the
+    reference's std::sort picks (the oracle makes the reference's call)."""
+    rng = np.random.default_rng(d * 100 + k)
+    xa = (np.round(rng.standard_normal(d * n) * 8) / 8).astype(np.float32)
+    xb = (np.round((0.5 * xa + rng.standard_normal(d * n)) * 8) / 8).astype(np.float32)
+    mi, det = oracle_mod.mi_pair(xa, xb, n, k, d, detail=True)
+    assert det["ties"] > 0
+    out = _mi_device(xa, xb, n, k, d)
+    for key in ("n_x", "n_y", "eps_x", "eps_y", "kdist"):
+        assert np.array_equal(out[key].cpu().numpy(), det[key]), key
+    assert float(out["mi"].item()) == mi

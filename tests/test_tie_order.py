@@ -1,0 +1,36 @@
+"""The sort-order replay used for tied samples (netsci_gb300/csrc/
+sort_prefix.h) against the host's std::sort, on random arrays with many
+equal keys (CPU only): the first T positions must hold the same indices in
+the same order."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_sort_prefix_matches_std_sort(tmp_path):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no g++")
+    exe = tmp_path / "sort_prefix_check"
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", str(ROOT / "netsci_gb300" / "csrc"),
+                    str(ROOT / "tests" / "native" / "sort_prefix_check.cpp"), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe), "6000"], capture_output=True, text=True, check=True).stdout
+    assert out.strip() == "ok 6000", out
+
+
+def test_oracle_counts_ties_on_coarse_grid(oracle_mod):
+    import numpy as np
+    rng = np.random.default_rng(0)
+    n, d, k = 800, 3, 6
+    xa = (np.round(rng.standard_normal(d * n) * 8) / 8).astype(np.float32)
+    xb = (np.round(rng.standard_normal(d * n) * 8) / 8).astype(np.float32)
+    mi, det = oracle_mod.mi_pair(xa, xb, n, k, d, detail=True)
+    assert det["ties"] > 20  # the coarse grid makes the neighbour order matter
+    R = oracle_mod.ref_lib()
+    if R is not None:
+        assert mi == R.ref_mi_cpu(xa, xb, n, k, d)
