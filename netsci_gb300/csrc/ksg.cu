@@ -51,6 +51,7 @@ int ksg_kmax_for(int k) {
     if (k + 1 <= 8) return 8;
     if (k + 1 <= 16) return 16;
     if (k + 1 <= 32) return 32;
+    if (k + 1 <= 64) return 64;
     return 0;
 }
 
@@ -90,6 +91,7 @@ int ksg_list_entries(int d, int kmax, const KsgKernelEntry** out, int cap) {
 
 KsgShape ksg_default_shape(int d, int kmax) {
     (void)d;
+    if (kmax >= 64) return {64, 1, 512};
     if (kmax >= 32) return {128, 1, 1024};
     if (kmax >= 16) return {128, 2, 1024};
     return {128, 2, 1024};

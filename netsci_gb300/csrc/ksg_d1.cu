@@ -14,6 +14,7 @@ const KsgKernelEntry kEntries[] = {
     NSG_KSG_FAMILY_SMALLK(1, 8, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K16(1, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K32(1, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_K64(1, NSG_KSG_VARIANT),
 };
 }  // namespace
 

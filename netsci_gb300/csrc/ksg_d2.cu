@@ -14,6 +14,7 @@ const KsgKernelEntry kEntries[] = {
     NSG_KSG_FAMILY_SMALLK(2, 8, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K16(2, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K32(2, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_K64(2, NSG_KSG_VARIANT),
 };
 }  // namespace
 

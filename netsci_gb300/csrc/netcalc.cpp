@@ -33,10 +33,22 @@ void check_variables(int xd, int d, int k, int n) {
     if (k < 1 || k >= n) invalid("k must satisfy 1 <= k < n");
 }
 
+// X of the pair-list calls: every node row must hold d*n values.
 void check_rows(CuArray<float>* X, int d, int n, const char* what) {
     if (!X || !X->allocatedHost() || !X->host()) invalid(std::string(what) + " has no host data");
     if (X->n() < d * n) {
         invalid(std::string(what) + " rows hold " + std::to_string(X->n()) +
+                " values; d*n = " + std::to_string(d * n) + " are needed");
+    }
+}
+
+// Xa / Xb of the per-pair calls: the buffer is read as d planes of n values
+// whatever its m x n shape (the reference indexes Xa[i + c*n] on the
+// contiguous host buffer), so it must hold d*n values in total.
+void check_variable(CuArray<float>* X, int d, int n, const char* what) {
+    if (!X || !X->allocatedHost() || !X->host()) invalid(std::string(what) + " has no host data");
+    if (X->size() < d * n) {
+        invalid(std::string(what) + " holds " + std::to_string(X->size()) +
                 " values; d*n = " + std::to_string(d * n) + " are needed");
     }
 }
@@ -195,15 +207,15 @@ int mutualInformation(CuArray<float>* X, CuArray<float>* I, CuArray<int>* ab, in
 
 float mutualInformationGpu(CuArray<float>* Xa, CuArray<float>* Xb, int k, int n, int xd, int d) {
     nsg::check_variables(xd, d, k, n);
-    nsg::check_rows(Xa, d, n, "Xa");
-    nsg::check_rows(Xb, d, n, "Xb");
+    nsg::check_variable(Xa, d, n, "Xa");
+    nsg::check_variable(Xb, d, n, "Xb");
     return nsg::gpu_single_pair(Xa, Xb, k, n, d);
 }
 
 float mutualInformationCpu(CuArray<float>* Xa, CuArray<float>* Xb, int k, int n, int xd, int d) {
     nsg::check_variables(xd, d, k, n);
-    nsg::check_rows(Xa, d, n, "Xa");
-    nsg::check_rows(Xb, d, n, "Xb");
+    nsg::check_variable(Xa, d, n, "Xa");
+    nsg::check_variable(Xb, d, n, "Xb");
     return nsg::ksg_cpu_pair(Xa->host(), Xb->host(), n, k, d);
 }
 

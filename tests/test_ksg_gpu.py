@@ -211,13 +211,13 @@ def test_edge_sizes_and_duplicates(oracle_mod):
 
 def test_invalid_k_statuses():
     from netsci_gb300 import NsgError, device
-    xa = np.random.default_rng(0).standard_normal(100).astype(np.float32)
-    X = _dev_pair(xa, xa, 1, 100)
+    xa = np.random.default_rng(0).standard_normal(200).astype(np.float32)
+    X = _dev_pair(xa, xa, 1, 200)
     with pytest.raises(NsgError) as e:
-        device.ksg_pair_detail(X[0], X[1], 100, 40, 1)
-    assert e.value.status == 4  # k > 32 unsupported on the GPU
+        device.ksg_pair_detail(X[0], X[1], 200, 70, 1)
+    assert e.value.status == 4  # k > 63 unsupported on the GPU
     with pytest.raises(NsgError) as e:
-        device.ksg_pair_detail(X[0], X[1], 100, 100, 1)
+        device.ksg_pair_detail(X[0], X[1], 200, 200, 1)
     assert e.value.status == 1  # k >= m
 
 
