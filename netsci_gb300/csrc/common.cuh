@@ -33,13 +33,23 @@ __device__ __forceinline__ float nsg_min3(float a, float b, float c) {
 
 // Packed pair subtraction: two IEEE round-to-nearest subtractions in one
 // instruction on sm_100+ (sub.rn.f32x2); bit-identical to two scalar FSUBs.
+// The operands are assembled and split with register-pair moves so no
+// extra arithmetic is generated around the packed instruction.
+__device__ __forceinline__ void nsg_sub2(float a0, float a1, float b0, float b1, float& r0,
+                                         float& r1) {
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\t"
+        "mov.b64 pa, {%2, %3};\n\t"
+        "mov.b64 pb, {%4, %5};\n\t"
+        "sub.rn.f32x2 pr, pa, pb;\n\t"
+        "mov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r0), "=f"(r1)
+        : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+
 __device__ __forceinline__ float2 nsg_sub2(float2 a, float2 b) {
-    unsigned long long ra, rb, rr;
-    ra = (static_cast<unsigned long long>(__float_as_uint(a.y)) << 32) | __float_as_uint(a.x);
-    rb = (static_cast<unsigned long long>(__float_as_uint(b.y)) << 32) | __float_as_uint(b.x);
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rr) : "l"(ra), "l"(rb));
-    return make_float2(__uint_as_float(static_cast<unsigned>(rr & 0xffffffffu)),
-                       __uint_as_float(static_cast<unsigned>(rr >> 32)));
+    float2 r;
+    nsg_sub2(a.x, a.y, b.x, b.y, r.x, r.y);
+    return r;
 }
 
 // Bounded mbarrier wait (phase parity). Returns false when the iteration

@@ -142,7 +142,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         maxm = std::max(maxm, q.m);
         total_samples += q.m;
     }
-    if (kmax_ == 0) fail(NSG_ERR_UNSUPPORTED, "k > 63 is not supported by the GPU path");
+    if (kmax_ == 0) fail(NSG_ERR_UNSUPPORTED, "k > 62 is not supported by the GPU path");
     const bool per_sample = out.nx || out.ny || out.eps_x || out.eps_y || out.kdist;
 
     // ---- tile shape -----------------------------------------------------

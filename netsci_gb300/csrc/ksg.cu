@@ -44,14 +44,13 @@ __global__ void ksg_final_kernel(KsgFinalArgs A) {
 
 }  // namespace
 
-// Smallest instantiated list length holding the k+1 nearest neighbours.
+// Smallest instantiated list length holding the sample itself and its k+1
+// nearest neighbours.
 int ksg_kmax_for(int k) {
     if (k < 1) return 0;
-    if (k + 1 <= 6) return 6;
-    if (k + 1 <= 8) return 8;
-    if (k + 1 <= 16) return 16;
-    if (k + 1 <= 32) return 32;
-    if (k + 1 <= 64) return 64;
+    for (int kmax : {6, 8, 16, 32, 64}) {
+        if (k + 2 <= kmax) return kmax;
+    }
     return 0;
 }
 
@@ -92,9 +91,8 @@ int ksg_list_entries(int d, int kmax, const KsgKernelEntry** out, int cap) {
 KsgShape ksg_default_shape(int d, int kmax) {
     (void)d;
     if (kmax >= 64) return {64, 1, 512};
-    if (kmax >= 32) return {128, 1, 1024};
-    if (kmax >= 16) return {128, 2, 1024};
-    return {128, 2, 1024};
+    if (kmax >= 16) return {128, 1, 1024};
+    return {256, 1, 1024};
 }
 
 bool ksg_shape_supported(int d, int kmax, const KsgShape& s) {

@@ -9,28 +9,32 @@
 //   * Pass 1 streams every frame j of the pair through a shared-memory tile
 //     (structure-of-arrays: one row of `frames` floats per coordinate plane),
 //     reads frames four at a time as float4 broadcasts, and forms the joint
-//     Chebyshev distance dz = max(d_a, d_b). A per-sample sorted list of the
-//     KMAX smallest (dz, j) lives in registers; it is only touched when the
-//     minimum dz of the four frames does not exceed the current k-th entry,
-//     which after the first few hundred frames is rare.
-//   * eps_a / eps_b are the largest marginal distances over the k list
-//     entries (netcalc/src/mutual_information_cpu.cpp:54-77).
+//     Chebyshev distance dz = max(d_a, d_b). A per-sample ascending list of
+//     the k+2 smallest (dz, j) -- the sample itself, whose dz is 0, and its
+//     k+1 nearest -- lives in registers; it is only touched when the minimum
+//     dz of the four frames is below the list's last entry, which after the
+//     first few hundred frames is rare, and then by one branch-free bubble
+//     step per candidate.
+//   * eps_a / eps_b are the largest marginal distances over list positions
+//     1..k (netcalc/src/mutual_information_cpu.cpp:54-77).
 //   * Pass 2 streams the frames again and counts d_a <= eps_a and
 //     d_b <= eps_b over all j (self included, then minus one,
 //     netcalc/src/mutual_information_cpu.cpp:78-109).
 //   * The sample's psi[n_x] + psi[n_y] (float add, :110) goes to the pair's
 //     scratch row; ksg_final_kernel sums the row in sample order.
 //
-// Runtime k < KMAX: the list keeps the k+1 nearest; its first KMAX-k-1 slots
-// hold (-inf, -1) sentinels that no candidate can displace, so the live
-// entries occupy the last k+1 slots and the admission threshold is always
-// slot KMAX-1 (a static register index).
+// Why the list needs no index tie-break: position 0 always holds a frame at
+// distance 0 (the sample itself or an exact duplicate, all with zero
+// marginals), and when the values at positions k and k+1 differ, positions
+// 1..k hold exactly the frames with dz <= that k-th value, whatever order
+// equal values were inserted in. When they are equal (and non-zero) the
+// reference's choice depends on its sort; the sample goes to the tie list
+// and ksg_tie_kernel recomputes it. Frames past m are staged as +inf and
+// never pass the strict admission test.
 //
-// Ties: candidates are ordered by (dz, j). That decides the neighbour set
-// exactly as the reference does whenever the k-th and (k+1)-th distances
-// differ (or are both zero: exact duplicates, whose marginals are zero).
-// Samples where they are equal are handed to ksg_tie_kernel, which replays
-// the reference sort's order for them.
+// Runtime k with KMAX >= k+2: the first KMAX-k-2 slots hold -inf sentinels
+// that never move, so the live entries occupy the last k+2 slots and the
+// admission threshold is always slot KMAX-1 (a static register index).
 //
 // Arithmetic: one rounded subtraction per coordinate, then exact abs/max, and
 // exact compares, so distances, eps and counts are bit-identical to the
@@ -43,23 +47,25 @@
 namespace nsg {
 namespace ksgk {
 
-__device__ __forceinline__ bool lex_less(float v, int j, float bv, int bj) {
-    return v < bv || (v == bv && j < bj);
-}
-
-// Insert (v, j) into the ascending list (bd, bj); the caller has checked
-// that (v, j) sorts before the last entry. Branch-free over the slots.
+// Insert (v, j) into the ascending list (bd, bj), dropping its last entry;
+// the caller has checked v < bd[KMAX-1]. Branch-free: place at the end,
+// then one compare-and-swap per slot towards the front. Sentinel slots
+// (-inf) never move.
 template <int KMAX>
-__device__ __forceinline__ void topk_insert(float (&bd)[KMAX], int (&bj)[KMAX], float v, int j) {
+__device__ __forceinline__ void list_insert(float (&bd)[KMAX], int (&bj)[KMAX], float v, int j) {
+    bd[KMAX - 1] = v;
+    bj[KMAX - 1] = j;
 #pragma unroll
-    for (int s = KMAX - 1; s >= 0; --s) {
-        const int p = s > 0 ? s - 1 : 0;
-        const bool lt_prev = (s > 0) && lex_less(v, j, bd[p], bj[p]);
-        const bool lt_cur = lex_less(v, j, bd[s], bj[s]);
-        const float nd = lt_prev ? bd[p] : (lt_cur ? v : bd[s]);
-        const int nj = lt_prev ? bj[p] : (lt_cur ? j : bj[s]);
-        bd[s] = nd;
-        bj[s] = nj;
+    for (int s = KMAX - 1; s > 0; --s) {
+        const bool sw = bd[s] < bd[s - 1];
+        const float lo = sw ? bd[s] : bd[s - 1];
+        const float hi = sw ? bd[s - 1] : bd[s];
+        const int jl = sw ? bj[s] : bj[s - 1];
+        const int jh = sw ? bj[s - 1] : bj[s];
+        bd[s - 1] = lo;
+        bd[s] = hi;
+        bj[s - 1] = jl;
+        bj[s] = jh;
     }
 }
 
@@ -172,17 +178,17 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
             }
         }
 
-        // k+1 live entries: the k nearest plus the next one, so that a tie
-        // between the k-th and (k+1)-th distance is visible.
+        // k+2 live entries: the sample itself (distance 0), the k nearest and
+        // the next one, so that a tie at the k-th distance is visible.
         float bd[R][KMAX];
         int bj[R][KMAX];
-        const int nsent = KMAX - (A.k + 1);
+        const int nsent = KMAX - (A.k + 2);
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
             for (int s = 0; s < KMAX; ++s) {
                 bd[r][s] = s < nsent ? -kInf : kInf;
-                bj[r][s] = s < nsent ? -1 : 0x7fffffff;
+                bj[r][s] = -1;
             }
 
         const int ntiles = (m + J - 1) / J;
@@ -220,14 +226,12 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
                     Marg<D, VARIANT>::four(qb[r], gb, db);
 #pragma unroll
                     for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
-                    const float mn = fminf(fminf(dz[0], dz[1]), fminf(dz[2], dz[3]));
-                    if (mn <= bd[r][KMAX - 1]) {
+                    const float mn = nsg_min3(dz[0], dz[1], fminf(dz[2], dz[3]));
+                    if (mn < bd[r][KMAX - 1]) {
 #pragma unroll
                         for (int f = 0; f < 4; ++f) {
-                            const int j = j0 + 4 * g + f;
-                            if (j < m && j != qi[r] &&
-                                lex_less(dz[f], j, bd[r][KMAX - 1], bj[r][KMAX - 1])) {
-                                topk_insert<KMAX>(bd[r], bj[r], dz[f], j);
+                            if (dz[f] < bd[r][KMAX - 1]) {
+                                list_insert<KMAX>(bd[r], bj[r], dz[f], j0 + 4 * g + f);
                             }
                         }
                     }
@@ -235,8 +239,9 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
             }
         }
 
-        // ---- eps from the k neighbours ---------------------------------------
-        // Slots nsent..KMAX-2 hold the k nearest. When the k-th distance
+        // ---- eps from list positions 1..k ---------------------------------------
+        // Position p is slot nsent+p; positions 1..k are slots nsent+1 ..
+        // KMAX-2 and position k+1 is slot KMAX-1. When the k-th distance
         // equals the (k+1)-th (and is not zero) the reference's choice among
         // the equal frames depends on its sort; such samples go to the tie
         // list and ksg_tie_kernel recomputes them.
@@ -255,9 +260,9 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
                 }
             }
 #pragma unroll
-            for (int s = 0; s < KMAX - 1; ++s) {
+            for (int s = 1; s < KMAX - 1; ++s) {
                 const int j = bj[r][s];
-                if (valid && j >= 0 && j < m) {
+                if (valid && s > nsent && j >= 0 && j < m) {
                     const int src = frame_of(fmap, j, ld, A.fault);
                     ea[r] = fmaxf(ea[r], marginal_at<D>(qa[r], xa, ld, src));
                     eb[r] = fmaxf(eb[r], marginal_at<D>(qb[r], xb, ld, src));

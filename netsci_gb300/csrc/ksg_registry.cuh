@@ -44,10 +44,9 @@ int ksg_list_entries(int d, int kmax, const KsgKernelEntry** out, int cap);
 
 // Standard shape family for one (D, KMAX) with variant V.
 #define NSG_KSG_FAMILY_SMALLK(D, KMAX, V)                                                   \
-    NSG_KSG_ENTRY(D, KMAX, 128, 2, 1024, V), NSG_KSG_ENTRY(D, KMAX, 128, 4, 512, V),        \
-        NSG_KSG_ENTRY(D, KMAX, 256, 1, 1024, V), NSG_KSG_ENTRY(D, KMAX, 64, 4, 512, V),     \
-        NSG_KSG_ENTRY(D, KMAX, 256, 2, 1024, V), NSG_KSG_ENTRY(D, KMAX, 64, 1, 512, V)
-#define NSG_KSG_FAMILY_K16(D, V)                                                            \
-    NSG_KSG_ENTRY(D, 16, 128, 2, 1024, V), NSG_KSG_ENTRY(D, 16, 128, 1, 1024, V)
+    NSG_KSG_ENTRY(D, KMAX, 256, 1, 1024, V), NSG_KSG_ENTRY(D, KMAX, 128, 1, 1024, V),       \
+        NSG_KSG_ENTRY(D, KMAX, 128, 2, 1024, V), NSG_KSG_ENTRY(D, KMAX, 256, 2, 1024, V),   \
+        NSG_KSG_ENTRY(D, KMAX, 64, 1, 512, V), NSG_KSG_ENTRY(D, KMAX, 512, 1, 1024, V)
+#define NSG_KSG_FAMILY_K16(D, V) NSG_KSG_ENTRY(D, 16, 128, 1, 1024, V)
 #define NSG_KSG_FAMILY_K32(D, V) NSG_KSG_ENTRY(D, 32, 128, 1, 1024, V)
 #define NSG_KSG_FAMILY_K64(D, V) NSG_KSG_ENTRY(D, 64, 64, 1, 512, V)
