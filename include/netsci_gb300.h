@@ -197,6 +197,24 @@ int nsg_ksg_plan_destroy(nsg_ksg_plan* plan);
  * process; threads == 0 restores automatic choice.                        */
 int nsg_ksg_set_shape(int threads, int r, int frames, int variant);
 
+/* One pair's MI / GC without any device allocation. No counterpart in the
+ * reference: it is for callers that cannot allocate device memory, such as
+ * an application that owns the GPU's memory through its own pool and calls
+ * this library as a plugin on its buffers, or a loop that cannot afford the
+ * synchronisation an allocation may cause. All scratch lives in a fixed
+ * NSG_NOALLOC_SCRATCH_BYTES device array inside the library, present on
+ * every GPU that loads it until the process exits. The first call on each
+ * device (with that device current) looks the array up and fills its psi
+ * table, so make it before any stream capture. Calls share the array:
+ * calls whose work overlaps on the GPU race. m is at most
+ * NSG_NOALLOC_MAX_SAMPLES (larger m: NSG_ERR_UNSUPPORTED). Rows as in
+ * nsg_ksg_pair_detail_device; mi, gc: device float[1] each, one nullable.
+ * Synchronizes `stream`.                                                  */
+#define NSG_NOALLOC_MAX_SAMPLES 65536
+#define NSG_NOALLOC_SCRATCH_BYTES 9454336
+int nsg_ksg_pair_noalloc_device(const float* xa, const float* xb, int ld, int m, int k, int d,
+                                float* mi, float* gc, void* stream);
+
 /* Hedetniemi shortest path lengths on the device (A, H: n x n device
  * floats). H_{t+1}[i][j] = min_k A[j][k] + H_t[k][i] from H_0 = A, until H
  * stops changing or max_path_length steps; the steps run go to *steps

@@ -98,6 +98,7 @@ _SIGNATURES = {
     "nsg_generate_psi": (c_int, [c_void_p, c_int]),
     "nsg_ksg_pairs_device": (c_int, [ctypes.POINTER(KsgPair), c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "nsg_ksg_pair_detail_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "nsg_ksg_pair_noalloc_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "nsg_ksg_plan_create": (c_int, [ctypes.POINTER(KsgPair), c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, PP_void]),
     "nsg_ksg_plan_run": (c_int, [c_void_p, c_void_p]),
     "nsg_ksg_plan_check": (c_int, [c_void_p]),

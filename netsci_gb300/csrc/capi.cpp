@@ -14,6 +14,7 @@
 #include "apsp.h"
 #include "cuarray.h"
 #include "engine.h"
+#include "ksg.cuh"
 #include "errors.h"
 #include "netcalc/generalized_correlation.h"
 #include "netcalc/hedetniemi.h"
@@ -411,6 +412,11 @@ int nsg_ksg_pair_detail_device(const float* xa, const float* xb, int ld, int m, 
         NSG_CUDA(cudaStreamSynchronize(stream_of(stream)));
         nsg::raise_fault(plan.take_fault());
     });
+}
+
+int nsg_ksg_pair_noalloc_device(const float* xa, const float* xb, int ld, int m, int k, int d,
+                                float* mi, float* gc, void* stream) {
+    return guarded([&] { nsg::ksg_pair_noalloc(xa, xb, ld, m, k, d, mi, gc, stream_of(stream)); });
 }
 
 int nsg_ksg_plan_create(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi, float* gc,

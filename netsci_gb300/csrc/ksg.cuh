@@ -106,6 +106,11 @@ void ksg_launch_final(const KsgFinalArgs& a, cudaStream_t st);
 // Warps the tie kernel runs with (scratch rows needed).
 int ksg_tie_warps();
 void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st);
+void ksg_launch_ties_ctas(const KsgTieArgs& a, int d, int ctas, cudaStream_t st);
+// One pair with all scratch in the library's static device area
+// (ksg_noalloc.cu); synchronizes s.
+void ksg_pair_noalloc(const float* xa, const float* xb, int ld, int m, int k, int d, float* mi,
+                      float* gc, cudaStream_t s);
 bool ksg_shape_supported(int d, int kmax, const KsgShape& s);
 
 }  // namespace nsg

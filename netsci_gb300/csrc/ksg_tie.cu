@@ -149,4 +149,17 @@ void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st) {
     NSG_CUDA(cudaGetLastError());
 }
 
+// The same kernel on a caller-chosen number of CTAs (the caller's scratch
+// holds kWarpsPerCta * ctas rows).
+void ksg_launch_ties_ctas(const KsgTieArgs& a, int d, int ctas, cudaStream_t st) {
+    const int threads = kWarpsPerCta * 32;
+    switch (d) {
+        case 1: ksg_tie_kernel<1><<<ctas, threads, 0, st>>>(a); break;
+        case 2: ksg_tie_kernel<2><<<ctas, threads, 0, st>>>(a); break;
+        case 3: ksg_tie_kernel<3><<<ctas, threads, 0, st>>>(a); break;
+        default: fail(NSG_ERR_INVALID, "d must be 1, 2 or 3");
+    }
+    NSG_CUDA(cudaGetLastError());
+}
+
 }  // namespace nsg
