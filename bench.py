@@ -214,7 +214,7 @@ def main():
     for s in range(S):
         gc = torch.empty(B, device="cuda")
         plans.append(device.KsgPlan(device.make_pairs(Xd, mm, slice_for(s)), K_NN, DIM, gc=gc,
-                                    graph=True, timing=True))
+                                    graph=True, timing=True, autotune=True))
         outs.append(gc)
     for s in range(args.warmup):
         plans[s].run()
@@ -342,7 +342,7 @@ def main():
                        "pairs_per_step": B, "total_pairs": int(len(ab_all)),
                        "parallelism": f"pairs sharded over {world} GPU(s), no collective",
                        "l2": "inputs larger than L2 (X resident, 241 MB > 129 MB L2)",
-                       "tile": None},
+                       "tile": plans[0].shape},
             "e2e": e2e, "plain_per_call": plain, "apsp": apsp,
             "gpu_launches": launches,
             "roofline": {"bound": "cuda_core_issue", "achieved": achieved,

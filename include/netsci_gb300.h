@@ -176,12 +176,20 @@ int nsg_ksg_pair_detail_device(const float* xa, const float* xb, int ld, int m, 
 /* Reusable plan: device descriptors, work queue and scratch built once;
  * each run is one captured CUDA graph (work-queue reset, count kernel,
  * finalize kernel per batch). Flags: bit 0 = capture a CUDA graph; bit 1 =
- * record CUDA events around every count launch (nsg_ksg_plan_count_ms).
+ * record CUDA events around every count launch (nsg_ksg_plan_count_ms);
+ * bit 2 = pick the tile shape with the autotuner (each instantiated shape
+ * timed on up to 512 of the pairs, longest first; the result is cached per
+ * (GPU, d, k bucket, m bucket, pair-count bucket), in the file named by the
+ * environment variable NSG_TUNE_CACHE when set).
  * The tile shape comes from the autotuner cache when one is loaded.       */
 typedef struct nsg_ksg_plan nsg_ksg_plan;
 int nsg_ksg_plan_create(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi,
                         float* gc, float* w, int flags, nsg_ksg_plan** out);
 int nsg_ksg_plan_run(nsg_ksg_plan* plan, void* stream);
+/* The tile shape a plan runs with (CTA threads, samples per thread, frames
+ * per tile, arithmetic variant); each pointer nullable.                   */
+int nsg_ksg_plan_shape(const nsg_ksg_plan* plan, int* threads, int* r, int* frames,
+                       int* variant);
 /* Raises NSG_ERR_DEVICE_FAULT when the runs so far recorded a device fault
  * (frame map entry out of range, tie list overflow); synchronizes.        */
 int nsg_ksg_plan_check(nsg_ksg_plan* plan);

@@ -102,6 +102,7 @@ _SIGNATURES = {
     "nsg_ksg_plan_create": (c_int, [ctypes.POINTER(KsgPair), c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, PP_void]),
     "nsg_ksg_plan_run": (c_int, [c_void_p, c_void_p]),
     "nsg_ksg_plan_check": (c_int, [c_void_p]),
+    "nsg_ksg_plan_shape": (c_int, [c_void_p, P_int, P_int, P_int, P_int]),
     "nsg_ksg_plan_launches": (c_int, [c_void_p, P_int]),
     "nsg_ksg_plan_count_ms": (c_int, [c_void_p, P_float]),
     "nsg_ksg_plan_destroy": (c_int, [c_void_p]),

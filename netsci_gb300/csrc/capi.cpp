@@ -432,6 +432,7 @@ int nsg_ksg_plan_create(const nsg_ksg_pair* pairs, int npairs, int k, int d, flo
         nsg::KsgPlanOptions opt;
         opt.graph = (flags & 1) != 0;
         opt.timing = (flags & 2) != 0;
+        opt.autotune = (flags & 4) != 0;
         *out = new nsg_ksg_plan{new nsg::KsgPlan(v, k, d, o, opt)};
     });
 }
@@ -440,6 +441,18 @@ int nsg_ksg_plan_run(nsg_ksg_plan* plan, void* stream) {
     return guarded([&] {
         if (!plan || !plan->plan) nsg::invalid("plan is null");
         plan->plan->run(stream_of(stream));
+    });
+}
+
+int nsg_ksg_plan_shape(const nsg_ksg_plan* plan, int* threads, int* r, int* frames,
+                       int* variant) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        const nsg::KsgShape& s = plan->plan->shape();
+        if (threads) *threads = s.threads;
+        if (r) *r = s.r;
+        if (frames) *frames = s.frames;
+        if (variant) *variant = plan->plan->variant();
     });
 }
 

@@ -2,7 +2,10 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -146,39 +149,50 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
     const bool per_sample = out.nx || out.ny || out.eps_x || out.eps_y || out.kdist;
 
     // ---- tile shape -----------------------------------------------------
-    {
+    // explicit per-plan shape, then the process-wide override, then the
+    // autotuner, then the preference order below
+    if (opt.shape.threads) {
+        shape_ = opt.shape;
+        variant_ = opt.variant;
+    } else {
         std::lock_guard<std::mutex> lk(g_shape_mu);
         if (g_forced.threads) {
             shape_ = g_forced;
             variant_ = g_forced_variant;
         }
     }
+    if (!shape_.threads && opt.autotune && npairs > 0) {
+        const KsgTuned t = ksg_autotune(pairs, k, d);
+        shape_ = t.shape;
+        variant_ = t.variant;
+    }
     if (shape_.threads) {
         if (!ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_)) {
-            fail(NSG_ERR_UNSUPPORTED, "forced KSG shape is not instantiated for this d/k");
+            fail(NSG_ERR_UNSUPPORTED, "requested KSG shape is not instantiated for this d/k");
         }
     } else {
-        // Largest per-CTA query block that still gives every resident CTA
-        // slot two work items; otherwise the smallest block.
+        // Preference: one sample per thread, CTAs near 256 threads (the best
+        // measured shapes at m = 10000); take the first preferred shape that
+        // gives every resident CTA slot two work items, else the shape with
+        // the smallest per-CTA sample block (small workloads).
         const KsgKernelEntry* cand[32];
         const int nc = std::min(32, ksg_list_entries(d, kmax_, cand, 32));
+        std::vector<const KsgKernelEntry*> pref;
+        for (int i = 0; i < nc; ++i) {
+            if (cand[i]->variant == cand[0]->variant) pref.push_back(cand[i]);  // default variant
+        }
+        std::stable_sort(pref.begin(), pref.end(), [](const KsgKernelEntry* a, const KsgKernelEntry* b) {
+            if (a->r != b->r) return a->r < b->r;
+            return std::abs(a->threads - 256) < std::abs(b->threads - 256);
+        });
         const int sms = sm_count();
         const KsgKernelEntry* best = nullptr;
-        long long best_q = -1;
         const KsgKernelEntry* smallest = nullptr;
-        const KsgShape pref = ksg_default_shape(d, kmax_);
-        for (int i = 0; i < nc; ++i) {
-            const KsgKernelEntry* e = cand[i];
-            if (e->variant != cand[0]->variant) continue;  // default variant family only
+        for (const KsgKernelEntry* e : pref) {
             const long long qc = static_cast<long long>(e->threads) * e->r;
             if (!smallest || qc < static_cast<long long>(smallest->threads) * smallest->r) smallest = e;
             const long long slots = static_cast<long long>(sms) * std::max(1, e->ctas_per_sm());
-            if (count_items(pairs, static_cast<int>(qc)) < 2 * slots) continue;
-            const bool is_pref = e->threads == pref.threads && e->r == pref.r && e->frames == pref.frames;
-            if (qc > best_q || (qc == best_q && is_pref)) {
-                best = e;
-                best_q = qc;
-            }
+            if (!best && count_items(pairs, static_cast<int>(qc)) >= 2 * slots) best = e;
         }
         if (!best) best = smallest;
         if (!best) fail(NSG_ERR_UNSUPPORTED, "no KSG kernel for this d/k");
@@ -344,6 +358,97 @@ int KsgPlan::take_fault() {
     NSG_CUDA(cudaMemcpy(&f, fault_.get(), sizeof(int), cudaMemcpyDeviceToHost));
     if (f) NSG_CUDA(cudaMemset(fault_.get(), 0, sizeof(int)));
     return f;
+}
+
+// ---------------------------------------------------------------------------
+// autotuner
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_tune_mu;
+std::map<std::string, KsgTuned> g_tune;
+bool g_tune_loaded = false;
+
+int bucket_pow2(long long v) {
+    int b = 0;
+    while ((1LL << b) < v) ++b;
+    return b;
+}
+
+std::string tune_key(int d, int kmax, int maxm, long long npairs) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, dev);
+    return std::string(prop.name) + "|d" + std::to_string(d) + "|K" + std::to_string(kmax) + "|m" +
+           std::to_string(bucket_pow2(maxm)) + "|p" + std::to_string(bucket_pow2(npairs));
+}
+
+void tune_load() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = std::getenv("NSG_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    char key[512];
+    KsgTuned t{};
+    while (std::fscanf(f, "%511[^\t]\t%d %d %d %d %lf\n", key, &t.shape.threads, &t.shape.r,
+                       &t.shape.frames, &t.variant, &t.gops) == 6) {
+        g_tune[key] = t;
+    }
+    std::fclose(f);
+}
+
+void tune_store(const std::string& key, const KsgTuned& t) {
+    const char* path = std::getenv("NSG_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE* f = std::fopen(path, "a");
+    if (!f) return;
+    std::fprintf(f, "%s\t%d %d %d %d %.3f\n", key.c_str(), t.shape.threads, t.shape.r,
+                 t.shape.frames, t.variant, t.gops);
+    std::fclose(f);
+}
+}  // namespace
+
+KsgTuned ksg_autotune(const std::vector<nsg_ksg_pair>& pairs, int k, int d) {
+    const int kmax = ksg_kmax_for(k);
+    int maxm = 0;
+    for (const auto& p : pairs) maxm = std::max(maxm, p.m);
+    const std::string key = tune_key(d, kmax, maxm, static_cast<long long>(pairs.size()));
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load();
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return it->second;
+    // probe: the longest pairs first, up to 512 of them
+    std::vector<nsg_ksg_pair> probe(pairs);
+    std::stable_sort(probe.begin(), probe.end(),
+                     [](const nsg_ksg_pair& a, const nsg_ksg_pair& b) { return a.m > b.m; });
+    if (probe.size() > 512) probe.resize(512);
+    double ops = 0;
+    for (const auto& p : probe) ops += 8.0 * d * p.m * (p.m - 1.0);
+    const KsgKernelEntry* cand[64];
+    const int nc = std::min(64, ksg_list_entries(d, kmax, cand, 64));
+    DeviceBuffer out(sizeof(float) * probe.size());
+    KsgTuned best{{0, 0, 0}, -1, -1.0};
+    for (int i = 0; i < nc; ++i) {
+        KsgPlanOptions o;
+        o.timing = true;
+        o.shape = {cand[i]->threads, cand[i]->r, cand[i]->frames};
+        o.variant = cand[i]->variant;
+        KsgOutputs ko;
+        ko.mi = out.as<float>();
+        KsgPlan plan(probe, k, d, ko, o);
+        plan.run(nullptr);
+        NSG_CUDA(cudaDeviceSynchronize());
+        plan.run(nullptr);
+        NSG_CUDA(cudaDeviceSynchronize());
+        const double ms = plan.count_ms();
+        const double gops = ms > 0 ? ops / ms / 1e6 : 0;
+        if (gops > best.gops) best = {o.shape, o.variant, gops};
+    }
+    g_tune[key] = best;
+    tune_store(key, best);
+    return best;
 }
 
 float KsgPlan::count_ms() const {

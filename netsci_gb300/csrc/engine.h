@@ -51,6 +51,9 @@ struct KsgOutputs {
 struct KsgPlanOptions {
     bool graph = false;                  // capture each run in a CUDA graph
     bool timing = false;                 // CUDA events around each count launch
+    bool autotune = false;               // time the instantiated shapes on a probe first
+    KsgShape shape{0, 0, 0};             // explicit shape (threads == 0: choose)
+    int variant = -1;
     size_t scratch_budget_bytes = 0;     // 0: library default
 };
 
@@ -100,6 +103,16 @@ private:
 std::shared_ptr<const DeviceBuffer> device_psi(int n);
 // Host psi table of the reference recurrence (netcalc/src/psi.cpp:6-20).
 void host_psi(float* psi, int n);
+
+// Best shape for a pair list, measured on a probe of its first pairs and
+// cached per (d, KMAX, m bucket, pair-count bucket); NSG_TUNE_CACHE names a
+// file that keeps the cache across processes.
+struct KsgTuned {
+    KsgShape shape;
+    int variant;
+    double gops;
+};
+KsgTuned ksg_autotune(const std::vector<nsg_ksg_pair>& pairs, int k, int d);
 
 // Shape override set by nsg_ksg_set_shape (threads == 0: automatic).
 void ksg_force_shape(int threads, int r, int frames, int variant);

@@ -97,11 +97,11 @@ class KsgPlan:
 
     def __init__(self, pairs: Sequence[KsgPair], k: int, d: int, mi: torch.Tensor | None = None,
                  gc: torch.Tensor | None = None, w: torch.Tensor | None = None,
-                 graph: bool = True, timing: bool = False):
+                 graph: bool = True, timing: bool = False, autotune: bool = False):
         self._keep = (mi, gc, w)
         arr = _pair_array(pairs)
         h = ctypes.c_void_p()
-        flags = (1 if graph else 0) | (2 if timing else 0)
+        flags = (1 if graph else 0) | (2 if timing else 0) | (4 if autotune else 0)
         call("nsg_ksg_plan_create", arr, len(pairs), int(k), int(d), _ptr(mi), _ptr(gc), _ptr(w),
              flags, ctypes.byref(h))
         self._h = h
@@ -118,6 +118,12 @@ class KsgPlan:
         v = ctypes.c_int()
         call("nsg_ksg_plan_launches", self._h, ctypes.byref(v))
         return v.value
+
+    @property
+    def shape(self) -> dict:
+        v = [ctypes.c_int() for _ in range(4)]
+        call("nsg_ksg_plan_shape", self._h, *(ctypes.byref(x) for x in v))
+        return dict(threads=v[0].value, r=v[1].value, frames=v[2].value, variant=v[3].value)
 
     def count_ms(self) -> float:
         """Device time (ms) of the count kernels in the last run."""

@@ -291,3 +291,19 @@ def test_tied_samples_follow_reference_sort_order(oracle_mod, d, k, n):
     for key in ("n_x", "n_y", "eps_x", "eps_y", "kdist"):
         assert np.array_equal(out[key].cpu().numpy(), det[key]), key
     assert float(out["mi"].item()) == mi
+
+
+def test_autotuned_plan_same_results_and_cached(tmp_path, monkeypatch):
+    from netsci_gb300 import device, synthetic
+    X, _ = synthetic.protein_trajectory(12, 900, seed=31)
+    Xd, m = device.pack_trajectory(X, 3)
+    pairs = device.make_pairs(Xd, m, synthetic.all_pairs(12))
+    a = torch.empty(len(pairs), device="cuda")
+    b = torch.empty(len(pairs), device="cuda")
+    device.KsgPlan(pairs, 6, 3, mi=a, graph=False).run()
+    tuned = device.KsgPlan(pairs, 6, 3, mi=b, graph=True, autotune=True)
+    tuned.run()
+    torch.cuda.synchronize()
+    assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
+    sh = tuned.shape
+    assert sh["threads"] in (64, 128, 256, 512) and sh["r"] in (1, 2)
