@@ -24,6 +24,11 @@ Lines reported (one JSON line from rank 0):
             8*d*m*(m-1) FP32 ops.
   cpu_baseline  the CPU oracle port (restatement of the reference CPU path)
             on all host cores, on a bounded sample of pairs of this workload.
+  uneven_batch  64 trajectories of uneven N and m in one plan vs the plain
+            per-pair call, and one shortest-path solve per trajectory.
+  bootstrap frame-resampled pairs of a 100-node subset (sampled resamples).
+  serving   a trace of the mixed request stream: continuous batching vs
+            one request at a time; p50/p99 latency and throughput.
 
 ``--impl reference`` runs only the CPU oracle port arm and prints its line.
 """
@@ -60,6 +65,12 @@ def parse():
     p.add_argument("--quick", action="store_true", help="small problem, for debugging")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=0, help="pairs in the CPU baseline sample")
+    p.add_argument("--c3-trajectories", type=int, default=64,
+                   help="uneven-batch configuration: trajectories (0 = skip)")
+    p.add_argument("--bootstrap-resamples", type=int, default=4,
+                   help="bootstrap sample: resamples of the 100-node subset (0 = skip)")
+    p.add_argument("--serving-requests", type=int, default=32,
+                   help="serving trace length (0 = skip)")
     return p.parse_args()
 
 
@@ -164,6 +175,128 @@ def reference_arm(args, rank: int):
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def uneven_batch(n_traj: int, quick: bool):
+    """Configuration C3: n_traj trajectories with N ~ U[50,500], m ~ U[500,5000]
+    (d=3, k=6); all pairs of all of them in one persistent plan (CUDA graph,
+    autotuned tile), against one netcalc.generalizedCorrelationGpu call per
+    pair (the reference's call structure) on a sample; then one Hedetniemi
+    solve per trajectory on its -ln(GC) contact graph."""
+    import torch
+    import cuarray
+    import netcalc
+    from netsci_gb300 import device, synthetic
+    scale = 0.2 if quick else 1.0
+    trajs = synthetic.uneven_batch(n_traj, n_range=(50, max(51, int(500 * scale))),
+                                   m_range=(500, max(501, int(5000 * scale))), seed=64)
+    keep, pairs, owners = [], [], []
+    for t, (X, mean) in enumerate(trajs):
+        Xd, m = device.pack_trajectory(X, DIM)
+        keep.append(Xd)
+        ab = synthetic.all_pairs(X.shape[0])
+        pairs += device.make_pairs(Xd, m, ab)
+        owners.append((len(pairs) - len(ab), len(ab)))
+    P = len(pairs)
+    gc = torch.empty(P, device="cuda")
+    w = torch.empty(P, device="cuda")
+    plan = device.KsgPlan(pairs, K_NN, DIM, gc=gc, w=w, graph=True, timing=True, autotune=True)
+    plan.run()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    plan.run()
+    ev1.record()
+    torch.cuda.synchronize()
+    batched_s = ev0.elapsed_time(ev1) / 1000.0
+    ops = sum(8.0 * DIM * p.m * (p.m - 1) for p in pairs)
+    # plain per-call sample
+    rng = np.random.default_rng(3)
+    sample = rng.choice(P, size=min(32, P), replace=False)
+    flat = [(t, a, b) for t, (X, _) in enumerate(trajs) for a, b in synthetic.all_pairs(X.shape[0])]
+    xs = []
+    for i in sample:
+        t, a, b = flat[i]
+        X = trajs[t][0]
+        xa, xb = cuarray.FloatCuArray(), cuarray.FloatCuArray()
+        xa.fromNumpy1D(X[a])
+        xb.fromNumpy1D(X[b])
+        xs.append((xa, xb, X.shape[1] // DIM, i))
+    netcalc.generalizedCorrelationGpu(Xa=xs[0][0], Xb=xs[0][1], k=K_NN, n=xs[0][2], xd=2, d=DIM)
+    t0 = time.perf_counter()
+    plain_ops = 0.0
+    for xa, xb, m, i in xs:
+        netcalc.generalizedCorrelationGpu(Xa=xa, Xb=xb, k=K_NN, n=m, xd=2, d=DIM)
+        plain_ops += 8.0 * DIM * m * (m - 1)
+    plain_s = time.perf_counter() - t0
+    # the plain rate is per pair of the sample; scale to the batch's pair mix by work
+    plain_pairs_per_s = len(xs) / plain_s * (plain_ops / len(xs)) / (ops / P)
+    # per-trajectory APSP on -ln(GC) contact graphs
+    gcv = gc.cpu().numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    apsp_steps = 0
+    for t, (X, mean) in enumerate(trajs):
+        off, cnt = owners[t]
+        A = synthetic.contact_graph(mean, gcv[off:off + cnt], synthetic.all_pairs(X.shape[0]))
+        H, st = device.apsp_lengths(torch.from_numpy(A).cuda(), X.shape[0])
+        apsp_steps += st
+    torch.cuda.synchronize()
+    apsp_s = time.perf_counter() - t0
+    return {"trajectories": n_traj, "pairs": P, "batched_pairs_per_s": P / batched_s,
+            "batched_s": batched_s, "batched_top_s": ops / batched_s / 1e12,
+            "plain_per_call_pairs_per_s": plain_pairs_per_s,
+            "speedup_vs_plain": (P / batched_s) / plain_pairs_per_s,
+            "plain_sample": f"{len(xs)} pairs, one netcalc.generalizedCorrelationGpu call each, "
+                            "rate scaled to the batch's mean work per pair",
+            "tile": plan.shape, "apsp_total_ms": 1000 * apsp_s, "apsp_steps": apsp_steps}
+
+
+def bootstrap(X, m, resamples: int):
+    """Bootstrap part of the large configuration: resamples of the frames
+    (with replacement, m' = m) of a fixed 100-node subset, all 4950 pairs per
+    resample in one plan (frame maps on the device)."""
+    import torch
+    from netsci_gb300 import device, synthetic
+    sub = np.ascontiguousarray(X[:100])
+    Xd, mm = device.pack_trajectory(sub, DIM)
+    rng = np.random.default_rng(100)
+    maps, pairs = [], []
+    ab = synthetic.all_pairs(100)
+    for r in range(resamples):
+        fm = torch.from_numpy(rng.integers(0, mm, size=mm).astype(np.int32)).cuda()
+        maps.append(fm)
+        pairs += device.make_pairs(Xd, mm, ab, fmap=fm, m_samples=mm)
+    gc = torch.empty(len(pairs), device="cuda")
+    plan = device.KsgPlan(pairs, K_NN, DIM, gc=gc, graph=True, autotune=True)
+    plan.run()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    plan.run()
+    ev1.record()
+    torch.cuda.synchronize()
+    dt = ev0.elapsed_time(ev1) / 1000.0
+    plan.check()
+    return {"resamples": resamples, "pairs": len(pairs), "pairs_per_s": len(pairs) / dt,
+            "full_job_estimate_s": 495000 / (len(pairs) / dt),
+            "note": "100 resamples x 4950 pairs is the full job; timed here on a sample"}
+
+
+def serving(n_req: int, quick: bool):
+    """Configuration C5: a trace of the mixed request stream replayed at its
+    arrival times against the continuous-batching server, and the same
+    requests one at a time through the plain per-request entry points."""
+    from netsci_gb300 import serving as sv
+    trace = sv.c5_trace(n_req, seed=5, rate=200.0, scale=0.25 if quick else 1.0)
+    with sv.Server(budget_bytes=150 << 30) as srv:
+        res_b, sum_b = sv.run_served(srv, trace)
+        st = srv.stats()
+    res_p, sum_p = sv.run_plain(trace)
+    same = all(np.array_equal(a, b) for a, b in zip(res_b, res_p))
+    return {"requests": n_req, "batched": sum_b, "plain": sum_p, "ticks": st["ticks"],
+            "peak_device_bytes": st["peak_bytes"], "results_equal_alone_and_mixed": same,
+            "budget_bytes": 150 << 30}
 
 
 def main():
@@ -322,6 +455,16 @@ def main():
             apsp[f"{name}_steps"] = steps
         apsp["n"] = n_g
 
+    # ---- other configurations (rank 0) ----------------------------------------------
+    extra = {}
+    if rank == 0:
+        if args.c3_trajectories:
+            extra["uneven_batch"] = uneven_batch(args.c3_trajectories, args.quick)
+        if args.bootstrap_resamples:
+            extra["bootstrap"] = bootstrap(X, m, args.bootstrap_resamples)
+        if args.serving_requests:
+            extra["serving"] = serving(args.serving_requests, args.quick)
+
     # ---- CPU baseline (oracle port on host cores) --------------------------------------
     cpu = None
     if rank == 0 and world == 1:
@@ -354,6 +497,7 @@ def main():
                                          f"{sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)")},
             "cpu_baseline": cpu, "clocks": clocks,
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
     for p in plans:
         p.close()

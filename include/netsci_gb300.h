@@ -239,6 +239,37 @@ int nsg_apsp_paths_device(const float* A, float* H, int* paths, int n, int max_p
  * r <= 0. Diagonal 0 in both.                                             */
 int nsg_corr_to_adjacency_device(const float* C, float* A, int n, int mode, void* stream);
 
+/* ---- 4. serving: continuous batching of MI / GC / APSP jobs ------------- */
+/* A request loop with no reference counterpart (the reference serves one
+ * blocking call at a time). Jobs are submitted from any thread with host
+ * input and output buffers that must stay valid until the job is done. A
+ * scheduler thread admits jobs when their device footprint fits
+ * budget_bytes and runs ticks of about tick_ops algorithmic operations, each
+ * one persistent launch over pairs of every admitted MI/GC job; jobs that
+ * arrive meanwhile join the next tick. APSP jobs run on their own stream.
+ * Registered trajectories stay resident in HBM. Job states: 0 pending,
+ * 1 running, 2 done, 3 failed. Times are seconds on the host steady clock. */
+typedef struct nsg_server nsg_server;
+int nsg_server_create(size_t budget_bytes, double tick_ops, int max_m, nsg_server** out);
+int nsg_server_destroy(nsg_server* s);
+/* X: host N x (d*m) plane-major rows, uploaded once and kept resident. */
+int nsg_server_register_trajectory(nsg_server* s, const float* X, int N, int m, int d,
+                                   int* traj);
+/* GC of all pairs a < b of a trajectory into out (host, N(N-1)/2 floats). */
+int nsg_server_submit_gc(nsg_server* s, int traj, int k, float* out, long long* job);
+/* MI of one pair (host x, y: d planes of n samples) into out (host float). */
+int nsg_server_submit_mi(nsg_server* s, const float* x, const float* y, int n, int d, int k,
+                         float* out, long long* job);
+/* Shortest path lengths of a host N x N matrix into out (host N*N floats). */
+int nsg_server_submit_apsp(nsg_server* s, const float* A, int N, int max_path_length,
+                           float* out, long long* job);
+/* Waits up to timeout_s for the job; *state as above. */
+int nsg_server_wait(nsg_server* s, long long job, double timeout_s, int* state);
+int nsg_server_job_info(nsg_server* s, long long job, int* state, double* submit_s,
+                        double* admit_s, double* done_s);
+int nsg_server_stats(nsg_server* s, long long* jobs_done, long long* pairs_done,
+                     long long* ticks, size_t* peak_bytes);
+
 #ifdef __cplusplus
 }
 #endif

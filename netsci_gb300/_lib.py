@@ -107,6 +107,15 @@ _SIGNATURES = {
     "nsg_ksg_plan_count_ms": (c_int, [c_void_p, P_float]),
     "nsg_ksg_plan_destroy": (c_int, [c_void_p]),
     "nsg_ksg_set_shape": (c_int, [c_int, c_int, c_int, c_int]),
+    "nsg_server_create": (c_int, [c_size_t, c_double, c_int, PP_void]),
+    "nsg_server_destroy": (c_int, [c_void_p]),
+    "nsg_server_register_trajectory": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, P_int]),
+    "nsg_server_submit_gc": (c_int, [c_void_p, c_int, c_int, c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "nsg_server_submit_mi": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "nsg_server_submit_apsp": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "nsg_server_wait": (c_int, [c_void_p, ctypes.c_longlong, c_double, P_int]),
+    "nsg_server_job_info": (c_int, [c_void_p, ctypes.c_longlong, P_int, P_double, P_double, P_double]),
+    "nsg_server_stats": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), P_size_t]),
     "nsg_apsp_lengths_device": (c_int, [c_void_p, c_void_p, c_int, c_int, P_int, c_void_p]),
     "nsg_apsp_paths_device": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_float, c_void_p]),
     "nsg_corr_to_adjacency_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p]),

@@ -177,10 +177,15 @@ void launch_step(const float* A, const float* H, float* Hn, int n, int* changed,
     NSG_CUDA(cudaGetLastError());
 }
 
+// Workspace allocated and freed in the order of the solver's stream, so a
+// solve does not wait for kernels on other streams.
 struct DevMem {
     void* p = nullptr;
-    explicit DevMem(size_t bytes) { NSG_CUDA(cudaMalloc(&p, bytes > 0 ? bytes : 1)); }
-    ~DevMem() { if (p) cudaFree(p); }
+    cudaStream_t s;
+    DevMem(size_t bytes, cudaStream_t st) : s(st) {
+        NSG_CUDA(cudaMallocAsync(&p, bytes > 0 ? bytes : 1, st));
+    }
+    ~DevMem() { if (p) cudaFreeAsync(p, s); }
     DevMem(const DevMem&) = delete;
     DevMem& operator=(const DevMem&) = delete;
 };
@@ -192,8 +197,8 @@ int apsp_lengths(const float* A, float* H, int n, int max_path_length, cudaStrea
     const size_t nn = (size_t)n * n;
     NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
     if (max_path_length == 0 || n == 0) return 0;
-    DevMem tmp(nn * sizeof(float));
-    DevMem changed(sizeof(int) * max_path_length);
+    DevMem tmp(nn * sizeof(float), s);
+    DevMem changed(sizeof(int) * max_path_length, s);
     NSG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int) * max_path_length, s));
     float* buf[2] = {H, static_cast<float*>(tmp.p)};
     int* ch = static_cast<int*>(changed.p);
@@ -232,9 +237,9 @@ void apsp_paths(const float* A, float* H, int* paths, int n, int L, float tolera
     const size_t nn = (size_t)n * n;
     NSG_CUDA(cudaMemsetAsync(paths, 0xff, sizeof(int) * nn * L, s));  // -1
     if (n == 0) return;
-    DevMem tmp(nn * sizeof(float));
-    DevMem snaps(nn * L * sizeof(float));
-    DevMem changed(sizeof(int) * L);
+    DevMem tmp(nn * sizeof(float), s);
+    DevMem snaps(nn * L * sizeof(float), s);
+    DevMem changed(sizeof(int) * L, s);
     NSG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int) * L, s));
     NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
     float* buf[2] = {H, static_cast<float*>(tmp.p)};

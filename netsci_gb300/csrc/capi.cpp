@@ -14,6 +14,7 @@
 #include "apsp.h"
 #include "cuarray.h"
 #include "engine.h"
+#include "serve.h"
 #include "ksg.cuh"
 #include "errors.h"
 #include "netcalc/generalized_correlation.h"
@@ -29,6 +30,10 @@ struct nsg_cuarray {
 
 struct nsg_ksg_plan {
     nsg::KsgPlan* plan;
+};
+
+struct nsg_server {
+    nsg::Server* server;
 };
 
 namespace {
@@ -506,6 +511,69 @@ int nsg_corr_to_adjacency_device(const float* C, float* A, int n, int mode, void
         if (mode != 0 && mode != 1) nsg::invalid("mode must be 0 (1/r) or 1 (-ln r)");
         nsg::corr_to_adjacency(C, A, n, mode, stream_of(stream));
     });
+}
+
+// ---- serving ---------------------------------------------------------------
+int nsg_server_create(size_t budget_bytes, double tick_ops, int max_m, nsg_server** out) {
+    return guarded([&] {
+        if (!out) nsg::invalid("out is null");
+        nsg::ServerConfig c;
+        if (budget_bytes) c.budget_bytes = budget_bytes;
+        if (tick_ops > 0) c.tick_ops = tick_ops;
+        if (max_m > 0) c.max_m = max_m;
+        *out = new nsg_server{new nsg::Server(c)};
+    });
+}
+
+int nsg_server_destroy(nsg_server* s) {
+    return guarded([&] {
+        if (!s) return;
+        delete s->server;
+        delete s;
+    });
+}
+
+int nsg_server_register_trajectory(nsg_server* s, const float* X, int N, int m, int d, int* traj) {
+    return guarded([&] { *traj = s->server->register_trajectory(X, N, m, d); });
+}
+
+int nsg_server_submit_gc(nsg_server* s, int traj, int k, float* out, long long* job) {
+    return guarded([&] { *job = s->server->submit_gc(traj, k, out); });
+}
+
+int nsg_server_submit_mi(nsg_server* s, const float* x, const float* y, int n, int d, int k,
+                         float* out, long long* job) {
+    return guarded([&] { *job = s->server->submit_mi(x, y, n, d, k, out); });
+}
+
+int nsg_server_submit_apsp(nsg_server* s, const float* A, int N, int L, float* out,
+                           long long* job) {
+    return guarded([&] { *job = s->server->submit_apsp(A, N, L, out); });
+}
+
+int nsg_server_wait(nsg_server* s, long long job, double timeout_s, int* state) {
+    return guarded([&] {
+        s->server->wait(job, timeout_s);
+        *state = s->server->state(job, nullptr);
+        if (*state == nsg::JOB_FAILED) nsg::fail(NSG_ERR_CUDA, "job failed: " + s->server->error(job));
+    });
+}
+
+int nsg_server_job_info(nsg_server* s, long long job, int* state, double* submit_s,
+                        double* admit_s, double* done_s) {
+    return guarded([&] {
+        nsg::JobTimes t;
+        const int st = s->server->state(job, &t);
+        if (state) *state = st;
+        if (submit_s) *submit_s = t.submit;
+        if (admit_s) *admit_s = t.admit;
+        if (done_s) *done_s = t.done;
+    });
+}
+
+int nsg_server_stats(nsg_server* s, long long* jobs_done, long long* pairs_done,
+                     long long* ticks, size_t* peak_bytes) {
+    return guarded([&] { s->server->stats(jobs_done, pairs_done, ticks, peak_bytes); });
 }
 
 }  // extern "C"
