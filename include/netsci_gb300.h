@@ -186,6 +186,8 @@ typedef struct nsg_ksg_plan nsg_ksg_plan;
 int nsg_ksg_plan_create(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi,
                         float* gc, float* w, int flags, nsg_ksg_plan** out);
 int nsg_ksg_plan_run(nsg_ksg_plan* plan, void* stream);
+/* Captures and instantiates a graph plan's CUDA graph without running it. */
+int nsg_ksg_plan_prepare(nsg_ksg_plan* plan);
 /* The tile shape a plan runs with (CTA threads, samples per thread, frames
  * per tile, arithmetic variant); each pointer nullable.                   */
 int nsg_ksg_plan_shape(const nsg_ksg_plan* plan, int* threads, int* r, int* frames,

@@ -101,6 +101,7 @@ _SIGNATURES = {
     "nsg_ksg_pair_noalloc_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "nsg_ksg_plan_create": (c_int, [ctypes.POINTER(KsgPair), c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, PP_void]),
     "nsg_ksg_plan_run": (c_int, [c_void_p, c_void_p]),
+    "nsg_ksg_plan_prepare": (c_int, [c_void_p]),
     "nsg_ksg_plan_check": (c_int, [c_void_p]),
     "nsg_ksg_plan_shape": (c_int, [c_void_p, P_int, P_int, P_int, P_int]),
     "nsg_ksg_plan_launches": (c_int, [c_void_p, P_int]),

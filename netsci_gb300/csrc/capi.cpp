@@ -468,6 +468,13 @@ int nsg_ksg_plan_check(nsg_ksg_plan* plan) {
     });
 }
 
+int nsg_ksg_plan_prepare(nsg_ksg_plan* plan) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        plan->plan->prepare();
+    });
+}
+
 int nsg_ksg_plan_launches(const nsg_ksg_plan* plan, int* launches) {
     return guarded([&] {
         if (!plan || !plan->plan) nsg::invalid("plan is null");

@@ -468,6 +468,12 @@ void KsgPlan::run(cudaStream_t s) {
         enqueue(s);
         return;
     }
+    prepare();
+    NSG_CUDA(cudaGraphLaunch(exec_, s));
+}
+
+void KsgPlan::prepare() {
+    if (!graph_) return;
     if (!exec_) {
         NSG_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
         NSG_CUDA(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
@@ -485,7 +491,6 @@ void KsgPlan::run(cudaStream_t s) {
         cudaGraphDestroy(g);
         NSG_CUDA(e);
     }
-    NSG_CUDA(cudaGraphLaunch(exec_, s));
 }
 
 }  // namespace nsg

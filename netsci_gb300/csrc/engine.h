@@ -63,6 +63,8 @@ public:
             const KsgPlanOptions& opt);
     ~KsgPlan();
     void run(cudaStream_t s);
+    // Captures and instantiates the run's CUDA graph now (graph plans only).
+    void prepare();
     // Kernel launches per run: count, tie resolution and finalize per batch.
     int launches() const { return 3 * static_cast<int>(batches_.size()); }
     // Device time of the count kernels of the last run (ms); needs timing.

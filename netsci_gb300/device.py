@@ -109,6 +109,10 @@ class KsgPlan:
     def run(self, stream: torch.cuda.Stream | None = None) -> None:
         call("nsg_ksg_plan_run", self._h, _stream(stream))
 
+    def prepare(self) -> None:
+        """Capture the CUDA graph now, so that the first run does not."""
+        call("nsg_ksg_plan_prepare", self._h)
+
     def check(self) -> None:
         """Raise NsgError when a run recorded a device fault."""
         call("nsg_ksg_plan_check", self._h)
