@@ -116,6 +116,18 @@ int sm_count() {
 // ---------------------------------------------------------------------------
 namespace {
 
+// Records `e` on `s`; while `s` is being captured the record becomes an
+// event node of the graph (cudaEventRecordExternal), otherwise a plain record.
+void record_event(cudaEvent_t e, cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    NSG_CUDA(cudaStreamIsCapturing(s, &st));
+    if (st == cudaStreamCaptureStatusActive) {
+        NSG_CUDA(cudaEventRecordWithFlags(e, s, cudaEventRecordExternal));
+    } else {
+        NSG_CUDA(cudaEventRecord(e, s));
+    }
+}
+
 long long count_items(const std::vector<nsg_ksg_pair>& pairs, int qc) {
     long long c = 0;
     for (const auto& p : pairs) c += (p.m + qc - 1) / qc;
@@ -314,12 +326,10 @@ void KsgPlan::enqueue(cudaStream_t s) {
         a.eps_x = out_.eps_x;
         a.eps_y = out_.eps_y;
         a.kdist = out_.kdist;
-        // External records stay real event nodes when the stream is captured.
-        if (timing_) NSG_CUDA(cudaEventRecordWithFlags(events_[2 * bi], s, cudaEventRecordExternal));
+        // Under capture, external records stay real event nodes in the graph.
+        if (timing_) record_event(events_[2 * bi], s);
         ksg_launch_counts(a, d_, kmax_, shape_, b.grid, s);
-        if (timing_) {
-            NSG_CUDA(cudaEventRecordWithFlags(events_[2 * bi + 1], s, cudaEventRecordExternal));
-        }
+        if (timing_) record_event(events_[2 * bi + 1], s);
         KsgTieArgs t{};
         t.pairs = pairs_dev_.as<KsgPairDesc>();
         t.ties = ties_.as<KsgTie>();

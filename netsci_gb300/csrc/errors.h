@@ -23,6 +23,7 @@ struct Error : std::runtime_error {
 
 inline void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) {
+        cudaGetLastError();  // a failed call also leaves its error pending; clear it
         fail(NSG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     }
 }
