@@ -192,6 +192,8 @@ int nsg_ksg_plan_prepare(nsg_ksg_plan* plan);
  * per tile, arithmetic variant); each pointer nullable.                   */
 int nsg_ksg_plan_shape(const nsg_ksg_plan* plan, int* threads, int* r, int* frames,
                        int* variant);
+/* Tile staging a plan runs with: 1 bulk copies (TMA), 0 plain loads.      */
+int nsg_ksg_plan_staging(const nsg_ksg_plan* plan, int* staging);
 /* Raises NSG_ERR_DEVICE_FAULT when the runs so far recorded a device fault
  * (frame map entry out of range, tie list overflow); synchronizes.        */
 int nsg_ksg_plan_check(nsg_ksg_plan* plan);
@@ -206,6 +208,11 @@ int nsg_ksg_plan_destroy(nsg_ksg_plan* plan);
  * arithmetic variant; variant < 0 = any) for subsequent calls in this
  * process; threads == 0 restores automatic choice.                        */
 int nsg_ksg_set_shape(int threads, int r, int frames, int variant);
+/* Tile staging for subsequent plans: 1 = bulk copies (TMA) into shared
+ * memory, 0 = plain loads, -1 = automatic (bulk copies when every pair has
+ * 16-byte aligned rows, a plane stride that is a multiple of 4 and no
+ * frame map).                                                             */
+int nsg_ksg_set_staging(int staging);
 
 /* One pair's MI / GC without any device allocation. No counterpart in the
  * reference: it is for callers that cannot allocate device memory, such as

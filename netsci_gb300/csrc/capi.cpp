@@ -461,6 +461,13 @@ int nsg_ksg_plan_shape(const nsg_ksg_plan* plan, int* threads, int* r, int* fram
     });
 }
 
+int nsg_ksg_plan_staging(const nsg_ksg_plan* plan, int* staging) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        *staging = plan->plan->staging();
+    });
+}
+
 int nsg_ksg_plan_check(nsg_ksg_plan* plan) {
     return guarded([&] {
         if (!plan || !plan->plan) nsg::invalid("plan is null");
@@ -499,6 +506,13 @@ int nsg_ksg_plan_destroy(nsg_ksg_plan* plan) {
 
 int nsg_ksg_set_shape(int threads, int r, int frames, int variant) {
     return guarded([&] { nsg::ksg_force_shape(threads, r, frames, variant); });
+}
+
+int nsg_ksg_set_staging(int staging) {
+    return guarded([&] {
+        if (staging < -1 || staging > 1) nsg::invalid("staging must be -1, 0 or 1");
+        nsg::ksg_force_staging(staging);
+    });
 }
 
 int nsg_apsp_lengths_device(const float* A, float* H, int n, int L, int* steps, void* stream) {

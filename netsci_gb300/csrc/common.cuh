@@ -73,3 +73,31 @@ __device__ __forceinline__ bool nsg_mbar_wait(uint32_t bar_smem, uint32_t parity
 __device__ __forceinline__ uint32_t nsg_smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
+
+// mbarrier and bulk-copy (TMA) primitives.
+__device__ __forceinline__ void nsg_mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+// Makes initialised barriers visible to the asynchronous (copy) proxy.
+__device__ __forceinline__ void nsg_fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Orders this thread's earlier shared-memory accesses before later
+// asynchronous-proxy accesses (a bulk copy into a buffer just read).
+__device__ __forceinline__ void nsg_fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Arrive on the barrier, announcing `bytes` of asynchronous transfers.
+__device__ __forceinline__ void nsg_mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+// One-dimensional bulk copy global -> shared, completing on `bar`.
+// dst and src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void nsg_bulk_load(uint32_t dst, const void* src, uint32_t bytes,
+                                              uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(dst), "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}

@@ -72,6 +72,7 @@ PsiCache g_psi[16];
 std::mutex g_shape_mu;
 KsgShape g_forced{0, 0, 0};
 int g_forced_variant = -1;
+int g_forced_staging = -1;
 }  // namespace
 
 std::shared_ptr<const DeviceBuffer> device_psi(int n) {
@@ -97,6 +98,20 @@ void ksg_force_shape(int threads, int r, int frames, int variant) {
     std::lock_guard<std::mutex> lk(g_shape_mu);
     g_forced = {threads, r, frames};
     g_forced_variant = variant;
+}
+
+void ksg_force_staging(int staging) {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    g_forced_staging = staging;
+}
+
+bool ksg_bulk_copy_ok(const std::vector<nsg_ksg_pair>& pairs) {
+    for (const auto& p : pairs) {
+        if (p.fmap) return false;
+        if ((reinterpret_cast<uintptr_t>(p.xa) | reinterpret_cast<uintptr_t>(p.xb)) & 15u) return false;
+        if (p.ld & 3) return false;
+    }
+    return !pairs.empty();
 }
 
 int sm_count() {
@@ -173,10 +188,12 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
             variant_ = g_forced_variant;
         }
     }
+    int tuned_staging = -1;
     if (!shape_.threads && opt.autotune && npairs > 0) {
         const KsgTuned t = ksg_autotune(pairs, k, d);
         shape_ = t.shape;
         variant_ = t.variant;
+        tuned_staging = t.staging;
     }
     if (shape_.threads) {
         if (!ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_)) {
@@ -191,7 +208,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         const int nc = std::min(32, ksg_list_entries(d, kmax_, cand, 32));
         std::vector<const KsgKernelEntry*> pref;
         for (int i = 0; i < nc; ++i) {
-            if (cand[i]->variant == cand[0]->variant) pref.push_back(cand[i]);  // default variant
+            if (cand[i]->variant == cand[0]->variant && !cand[i]->tma) pref.push_back(cand[i]);
         }
         std::stable_sort(pref.begin(), pref.end(), [](const KsgKernelEntry* a, const KsgKernelEntry* b) {
             if (a->r != b->r) return a->r < b->r;
@@ -211,7 +228,27 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         shape_ = {best->threads, best->r, best->frames};
         variant_ = best->variant;
     }
-    const KsgKernelEntry* entry = ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_);
+    // staging: plain loads unless the plan option, the override or the
+    // autotuner asks for bulk copies (which need aligned rows and no frame map)
+    int staging = opt.staging;
+    if (staging < 0) {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        staging = g_forced_staging;
+    }
+    if (staging < 0) staging = tuned_staging;
+    if (staging < 0) staging = 0;
+    const bool bulk_ok = ksg_bulk_copy_ok(pairs);
+    const KsgKernelEntry* entry = nullptr;
+    if (staging != 0 && bulk_ok) {
+        entry = ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_, 1);
+    }
+    if (staging == 1 && !entry) {
+        fail(NSG_ERR_UNSUPPORTED, bulk_ok ? "no bulk-copy kernel for this shape"
+                                          : "bulk-copy staging needs aligned rows and no frame map");
+    }
+    if (!entry) entry = ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_, 0);
+    if (!entry) fail(NSG_ERR_UNSUPPORTED, "no KSG kernel instantiated for this shape");
+    entry_ = entry;
     variant_ = entry->variant;
     const int qc = shape_.threads * shape_.r;
 
@@ -257,7 +294,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
             ++pos;
         }
         b.nitems = static_cast<int>(items.size()) - b.item0;
-        const int slots = sm_count() * std::max(1, entry->ctas_per_sm());
+        const int slots = sm_count() * std::max(1, entry_->ctas_per_sm());
         b.grid = std::max(1, std::min(b.nitems, slots));
         scratch_need = std::max(scratch_need, per_sample ? total_samples : used);
         batches_.push_back(b);
@@ -273,8 +310,9 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         scratch_.reset(static_cast<size_t>(scratch_need) * sizeof(float));
         // per batch: work-queue head, tie count, tie-kernel work counter
         counters_.reset(3 * batches_.size() * sizeof(int));
-        // Tied samples are rare (about 1e-4 of samples on trajectory data);
-        // the list holds 1/16 of the largest batch's samples.
+        // Samples with an ambiguous tie are rare (about 1e-4 on trajectory
+        // data; ties among copies of one frame are not listed); the list
+        // holds a quarter of the largest batch's samples.
         long long batch_samples = 0;
         for (const Batch& b : batches_) {
             long long sum = 0;
@@ -282,7 +320,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
             batch_samples = std::max(batch_samples, sum);
         }
         tie_cap_ = static_cast<int>(std::min<long long>(
-            std::max<long long>(65536, batch_samples / 16), 1LL << 30));
+            std::max<long long>(65536, batch_samples / 4), 1LL << 30));
         ties_.reset(static_cast<size_t>(tie_cap_) * sizeof(KsgTie));
         tie_stride_ = maxm;
         tie_dz_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(float));
@@ -328,7 +366,8 @@ void KsgPlan::enqueue(cudaStream_t s) {
         a.kdist = out_.kdist;
         // Under capture, external records stay real event nodes in the graph.
         if (timing_) record_event(events_[2 * bi], s);
-        ksg_launch_counts(a, d_, kmax_, shape_, b.grid, s);
+        entry_->launch(a, b.grid, s);
+        NSG_CUDA(cudaGetLastError());
         if (timing_) record_event(events_[2 * bi + 1], s);
         KsgTieArgs t{};
         t.pairs = pairs_dev_.as<KsgPairDesc>();
@@ -361,6 +400,8 @@ void KsgPlan::enqueue(cudaStream_t s) {
         ksg_launch_final(f, s);
     }
 }
+
+int KsgPlan::staging() const { return entry_ ? entry_->tma : 0; }
 
 int KsgPlan::take_fault() {
     if (!fault_.get()) return FAULT_NONE;
@@ -402,8 +443,8 @@ void tune_load() {
     if (!f) return;
     char key[512];
     KsgTuned t{};
-    while (std::fscanf(f, "%511[^\t]\t%d %d %d %d %lf\n", key, &t.shape.threads, &t.shape.r,
-                       &t.shape.frames, &t.variant, &t.gops) == 6) {
+    while (std::fscanf(f, "%511[^\t]\t%d %d %d %d %d %lf\n", key, &t.shape.threads, &t.shape.r,
+                       &t.shape.frames, &t.variant, &t.staging, &t.gops) == 7) {
         g_tune[key] = t;
     }
     std::fclose(f);
@@ -414,8 +455,8 @@ void tune_store(const std::string& key, const KsgTuned& t) {
     if (!path || !*path) return;
     FILE* f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "%s\t%d %d %d %d %.3f\n", key.c_str(), t.shape.threads, t.shape.r,
-                 t.shape.frames, t.variant, t.gops);
+    std::fprintf(f, "%s\t%d %d %d %d %d %.3f\n", key.c_str(), t.shape.threads, t.shape.r,
+                 t.shape.frames, t.variant, t.staging, t.gops);
     std::fclose(f);
 }
 }  // namespace
@@ -438,13 +479,16 @@ KsgTuned ksg_autotune(const std::vector<nsg_ksg_pair>& pairs, int k, int d) {
     for (const auto& p : probe) ops += 8.0 * d * p.m * (p.m - 1.0);
     const KsgKernelEntry* cand[64];
     const int nc = std::min(64, ksg_list_entries(d, kmax, cand, 64));
+    const bool bulk_ok = ksg_bulk_copy_ok(probe);
     DeviceBuffer out(sizeof(float) * probe.size());
-    KsgTuned best{{0, 0, 0}, -1, -1.0};
+    KsgTuned best{{0, 0, 0}, -1, 0, -1.0};
     for (int i = 0; i < nc; ++i) {
+        if (cand[i]->tma && !bulk_ok) continue;
         KsgPlanOptions o;
         o.timing = true;
         o.shape = {cand[i]->threads, cand[i]->r, cand[i]->frames};
         o.variant = cand[i]->variant;
+        o.staging = cand[i]->tma;
         KsgOutputs ko;
         ko.mi = out.as<float>();
         KsgPlan plan(probe, k, d, ko, o);
@@ -454,7 +498,7 @@ KsgTuned ksg_autotune(const std::vector<nsg_ksg_pair>& pairs, int k, int d) {
         NSG_CUDA(cudaDeviceSynchronize());
         const double ms = plan.count_ms();
         const double gops = ms > 0 ? ops / ms / 1e6 : 0;
-        if (gops > best.gops) best = {o.shape, o.variant, gops};
+        if (gops > best.gops) best = {o.shape, o.variant, o.staging, gops};
     }
     g_tune[key] = best;
     tune_store(key, best);

@@ -54,6 +54,7 @@ struct KsgPlanOptions {
     bool autotune = false;               // time the instantiated shapes on a probe first
     KsgShape shape{0, 0, 0};             // explicit shape (threads == 0: choose)
     int variant = -1;
+    int staging = -1;                    // -1 auto, 0 plain loads, 1 bulk copies (TMA)
     size_t scratch_budget_bytes = 0;     // 0: library default
 };
 
@@ -74,6 +75,7 @@ public:
     int take_fault();
     const KsgShape& shape() const { return shape_; }
     int variant() const { return variant_; }
+    int staging() const;  // 1: bulk-copy staged kernel, 0: plain loads
 
 private:
     struct Batch {
@@ -89,6 +91,7 @@ private:
     std::vector<cudaEvent_t> events_;
     KsgShape shape_{};
     int variant_ = -1;
+    const struct KsgKernelEntry* entry_ = nullptr;
     KsgOutputs out_;
     std::vector<Batch> batches_;
     DeviceBuffer pairs_dev_, items_dev_, scratch_, counters_, fault_;
@@ -112,12 +115,18 @@ void host_psi(float* psi, int n);
 struct KsgTuned {
     KsgShape shape;
     int variant;
+    int staging;
     double gops;
 };
 KsgTuned ksg_autotune(const std::vector<nsg_ksg_pair>& pairs, int k, int d);
 
 // Shape override set by nsg_ksg_set_shape (threads == 0: automatic).
 void ksg_force_shape(int threads, int r, int frames, int variant);
+// Staging override set by nsg_ksg_set_staging (-1 automatic).
+void ksg_force_staging(int staging);
+// True when every pair allows bulk-copy staging (16-byte aligned rows,
+// plane stride a multiple of 4, no frame map).
+bool ksg_bulk_copy_ok(const std::vector<nsg_ksg_pair>& pairs);
 int sm_count();
 
 }  // namespace nsg

@@ -64,12 +64,13 @@ static const KsgKernelEntry* entries_for(int d, int* count) {
 }
 
 const KsgKernelEntry* ksg_find_entry(int d, int kmax, int threads, int r, int frames,
-                                     int variant) {
+                                     int variant, int tma) {
     int n = 0;
     const KsgKernelEntry* e = entries_for(d, &n);
     for (int i = 0; i < n; ++i) {
         if (e[i].kmax == kmax && e[i].threads == threads && e[i].r == r &&
-            e[i].frames == frames && (variant < 0 || e[i].variant == variant)) {
+            e[i].frames == frames && (variant < 0 || e[i].variant == variant) &&
+            (tma < 0 || e[i].tma == tma)) {
             return &e[i];
         }
     }

@@ -15,6 +15,8 @@ const KsgKernelEntry kEntries[] = {
     NSG_KSG_FAMILY_K16(1, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K32(1, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K64(1, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_TMA(1, 6, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_TMA(1, 8, NSG_KSG_VARIANT),
 };
 }  // namespace
 

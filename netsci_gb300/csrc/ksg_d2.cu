@@ -15,6 +15,8 @@ const KsgKernelEntry kEntries[] = {
     NSG_KSG_FAMILY_K16(2, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K32(2, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K64(2, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_TMA(2, 6, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_TMA(2, 8, NSG_KSG_VARIANT),
 };
 }  // namespace
 

@@ -15,6 +15,8 @@ const KsgKernelEntry kEntries[] = {
     NSG_KSG_FAMILY_K16(3, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K32(3, NSG_KSG_VARIANT),
     NSG_KSG_FAMILY_K64(3, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_TMA(3, 6, NSG_KSG_VARIANT),
+    NSG_KSG_FAMILY_TMA(3, 8, NSG_KSG_VARIANT),
     // arithmetic variants of the d=3, k<=8 family, kept for the tuner
     NSG_KSG_FAMILY_SMALLK(3, 8, 0),
     NSG_KSG_FAMILY_SMALLK(3, 8, 2),

@@ -141,13 +141,223 @@ __device__ __forceinline__ float marginal_at(const float (&q)[D], const float* _
     return v;
 }
 
+// ---- per-tile pieces shared by the staged kernels -----------------------------
+
+// Pass 1 over one tile: planes of the tile at tile[c*stride + f], frames
+// j0 .. j0+jn-1 (frames past the pair's end hold +inf).
+template <int D, int KMAX, int R, int VARIANT>
+__device__ __forceinline__ void pass1_tile(const float* tile, int stride, int j0, int jn,
+                                           const float (&qa)[R][D], const float (&qb)[R][D],
+                                           float (&bd)[R][KMAX], int (&bj)[R][KMAX]) {
+    const int ngroups = (jn + 3) >> 2;
+    for (int g = 0; g < ngroups; ++g) {
+        float4 ga[D], gb[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            ga[c] = *reinterpret_cast<const float4*>(tile + c * stride + 4 * g);
+            gb[c] = *reinterpret_cast<const float4*>(tile + (D + c) * stride + 4 * g);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            float da[4], db[4], dz[4];
+            Marg<D, VARIANT>::four(qa[r], ga, da);
+            Marg<D, VARIANT>::four(qb[r], gb, db);
+#pragma unroll
+            for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
+            const float mn = nsg_min3(dz[0], dz[1], fminf(dz[2], dz[3]));
+            if (mn < bd[r][KMAX - 1]) {
+#pragma unroll
+                for (int f = 0; f < 4; ++f) {
+                    if (dz[f] < bd[r][KMAX - 1]) {
+                        list_insert<KMAX>(bd[r], bj[r], dz[f], j0 + 4 * g + f);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Pass 2 over one tile: marginal counts against eps. With CHECK, also
+// looks at every frame whose joint distance equals a flagged sample's k-th
+// distance wk and records in `mixed` whether any of them has marginals other
+// than (ra, rb) -- the only case in which the reference's choice among tied
+// frames can change eps.
+template <int D, int R, int VARIANT, bool CHECK>
+__device__ __forceinline__ void pass2_tile(const float* tile, int stride, int jn,
+                                           const float (&qa)[R][D], const float (&qb)[R][D],
+                                           const float (&ea)[R], const float (&eb)[R],
+                                           int (&ca)[R], int (&cb)[R], const float (&wk)[R],
+                                           const float (&ra)[R], const float (&rb)[R],
+                                           bool (&mixed)[R]) {
+    const int ngroups = (jn + 3) >> 2;
+    for (int g = 0; g < ngroups; ++g) {
+        float4 ga[D], gb[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            ga[c] = *reinterpret_cast<const float4*>(tile + c * stride + 4 * g);
+            gb[c] = *reinterpret_cast<const float4*>(tile + (D + c) * stride + 4 * g);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            float da[4], db[4];
+            Marg<D, VARIANT>::four(qa[r], ga, da);
+            Marg<D, VARIANT>::four(qb[r], gb, db);
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                ca[r] += da[f] <= ea[r] ? 1 : 0;
+                cb[r] += db[f] <= eb[r] ? 1 : 0;
+                if constexpr (CHECK) {
+                    if (fmaxf(da[f], db[f]) == wk[r] && (da[f] != ra[r] || db[f] != rb[r])) {
+                        mixed[r] = true;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Query samples of this thread and their empty neighbour lists.
+template <int D, int KMAX, int R, int NT>
+__device__ __forceinline__ void load_queries(const KsgCountArgs& A, const KsgItem& w,
+                                             const KsgPairDesc& P, int tid, float (&qa)[R][D],
+                                             float (&qb)[R][D], int (&qi)[R],
+                                             float (&bd)[R][KMAX], int (&bj)[R][KMAX]) {
+    const float kInf = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        qi[r] = w.q0 + r * NT + tid;
+        const bool valid = qi[r] < w.q1;
+        const int src = valid ? frame_of(P.fmap, qi[r], P.ld, A.fault) : 0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            qa[r][c] = valid ? __ldg(P.xa + (size_t)c * P.ld + src) : 0.f;
+            qb[r][c] = valid ? __ldg(P.xb + (size_t)c * P.ld + src) : 0.f;
+        }
+    }
+    // k+2 live entries: the sample itself (distance 0), the k nearest and
+    // the next one, so that a tie at the k-th distance is visible.
+    const int nsent = KMAX - (A.k + 2);
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int s = 0; s < KMAX; ++s) {
+            bd[r][s] = s < nsent ? -kInf : kInf;
+            bj[r][s] = -1;
+        }
+}
+
+// eps from list positions 1..k, and the tie test. Position p is slot
+// nsent+p; positions 1..k are slots nsent+1 .. KMAX-2 and position k+1 is
+// slot KMAX-1. A sample is flagged when its k-th distance equals its
+// (k+1)-th and is not zero: then the reference's choice among the frames at
+// that distance comes from its sort. (ra, rb) are the marginals of the
+// frame at position k; pass 2 checks whether every frame at distance wk has
+// the same ones (for example copies of one frame in a bootstrap resample),
+// in which case the choice cannot change eps and the flag is dropped.
+template <int D, int KMAX, int R>
+__device__ __forceinline__ void eps_and_ties(const KsgCountArgs& A, const KsgItem& w,
+                                             const KsgPairDesc& P, const float (&qa)[R][D],
+                                             const float (&qb)[R][D], const int (&qi)[R],
+                                             const float (&bd)[R][KMAX], const int (&bj)[R][KMAX],
+                                             float (&ea)[R], float (&eb)[R], bool (&tie)[R],
+                                             float (&wk)[R], float (&ra)[R], float (&rb)[R]) {
+    const int nsent = KMAX - (A.k + 2);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        ea[r] = 0.f;
+        eb[r] = 0.f;
+        ra[r] = 0.f;
+        rb[r] = 0.f;
+        const bool valid = qi[r] < w.q1;
+        wk[r] = bd[r][KMAX - 2];
+        tie[r] = valid && bd[r][KMAX - 2] == bd[r][KMAX - 1] && bd[r][KMAX - 2] > 0.f;
+#pragma unroll
+        for (int s = 1; s < KMAX - 1; ++s) {
+            const int j = bj[r][s];
+            if (valid && s > nsent && j >= 0 && j < P.m) {
+                const int src = frame_of(P.fmap, j, P.ld, A.fault);
+                const float da = marginal_at<D>(qa[r], P.xa, P.ld, src);
+                const float db = marginal_at<D>(qb[r], P.xb, P.ld, src);
+                ea[r] = fmaxf(ea[r], da);
+                eb[r] = fmaxf(eb[r], db);
+                if (s == KMAX - 2) {
+                    ra[r] = da;
+                    rb[r] = db;
+                }
+            }
+        }
+    }
+}
+
+// Samples whose tied frames differ in their marginals go to the tie list
+// (ksg_tie_kernel recomputes them with the reference sort's order).
+template <int R>
+__device__ __forceinline__ void report_ties(const KsgCountArgs& A, const KsgItem& w,
+                                            const int (&qi)[R], const bool (&tie)[R],
+                                            const bool (&mixed)[R]) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (tie[r] && mixed[r]) {
+            const int slot = atomicAdd(A.tie_count, 1);
+            if (slot < A.tie_cap) {
+                A.ties[slot] = KsgTie{w.pair, qi[r]};
+            } else {
+                atomicOr(A.fault, FAULT_TIE_OVERFLOW);
+            }
+        }
+    }
+}
+
+template <int KMAX, int R>
+__device__ __forceinline__ void write_outputs(const KsgCountArgs& A, const KsgItem& w,
+                                              const KsgPairDesc& P, const int (&qi)[R],
+                                              const float (&bd)[R][KMAX], const float (&ea)[R],
+                                              const float (&eb)[R], const int (&ca)[R],
+                                              const int (&cb)[R]) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (qi[r] < w.q1) {
+            const long long o = P.scratch + qi[r];
+            // counts lie in [k, m-1] for finite inputs; the clamp keeps
+            // non-finite inputs from indexing outside the psi table
+            const int nx = min(max(ca[r] - 1, 0), P.m);
+            const int ny = min(max(cb[r] - 1, 0), P.m);
+            A.psum[o] = __fadd_rn(__ldg(A.psi + nx), __ldg(A.psi + ny));
+            if (A.nx) A.nx[o] = nx;
+            if (A.ny) A.ny[o] = ny;
+            if (A.eps_x) A.eps_x[o] = ea[r];
+            if (A.eps_y) A.eps_y[o] = eb[r];
+            if (A.kdist) A.kdist[o] = bd[r][KMAX - 2];
+        }
+    }
+}
+
+// Staging with plain loads: every thread copies part of the tile
+// (frame maps gathered here), frames past the pair's end set to +inf.
+template <int D, int NT, int J>
+__device__ __forceinline__ void stage_tile(float (&tile)[2 * D][J], const KsgPairDesc& P, int j0,
+                                           int tid, int* fault) {
+    const float kInf = __int_as_float(0x7f800000);
+    for (int idx = tid; idx < 2 * D * J; idx += NT) {
+        const int c = idx / J;
+        const int f = idx - c * J;
+        const int j = j0 + f;
+        float v = kInf;
+        if (j < P.m) {
+            const int src = frame_of(P.fmap, j, P.ld, fault);
+            v = c < D ? __ldg(P.xa + (size_t)c * P.ld + src)
+                      : __ldg(P.xb + (size_t)(c - D) * P.ld + src);
+        }
+        tile[c][f] = v;
+    }
+}
+
 template <int D, int KMAX, int R, int NT, int J, int VARIANT>
 __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
     static_assert(J % (4 * 32) == 0, "tile must hold whole float4 groups");
     __shared__ __align__(16) float tile[2 * D][J];
     __shared__ int s_item;
     const int tid = threadIdx.x;
-    const float kInf = __int_as_float(0x7f800000);
 
     for (;;) {
         if (tid == 0) s_item = atomicAdd(A.counter, 1);
@@ -158,117 +368,33 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
         const KsgItem w = A.items[item];
         const KsgPairDesc P = A.pairs[w.pair];
         const int m = P.m;
-        const int ld = P.ld;
-        const int* __restrict__ fmap = P.fmap;
-        const float* __restrict__ xa = P.xa;
-        const float* __restrict__ xb = P.xb;
 
-        // query samples of this thread
         float qa[R][D], qb[R][D];
         int qi[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            qi[r] = w.q0 + r * NT + tid;
-            const bool valid = qi[r] < w.q1;
-            const int src = valid ? frame_of(fmap, qi[r], ld, A.fault) : 0;
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                qa[r][c] = valid ? __ldg(xa + (size_t)c * ld + src) : 0.f;
-                qb[r][c] = valid ? __ldg(xb + (size_t)c * ld + src) : 0.f;
-            }
-        }
-
-        // k+2 live entries: the sample itself (distance 0), the k nearest and
-        // the next one, so that a tie at the k-th distance is visible.
         float bd[R][KMAX];
         int bj[R][KMAX];
-        const int nsent = KMAX - (A.k + 2);
-#pragma unroll
-        for (int r = 0; r < R; ++r)
-#pragma unroll
-            for (int s = 0; s < KMAX; ++s) {
-                bd[r][s] = s < nsent ? -kInf : kInf;
-                bj[r][s] = -1;
-            }
+        load_queries<D, KMAX, R, NT>(A, w, P, tid, qa, qb, qi, bd, bj);
 
         const int ntiles = (m + J - 1) / J;
-
         // ---- pass 1: k nearest joint neighbours ------------------------------
         for (int t = 0; t < ntiles; ++t) {
             const int j0 = t * J;
             __syncthreads();
-            for (int idx = tid; idx < 2 * D * J; idx += NT) {
-                const int c = idx / J;
-                const int f = idx - c * J;
-                const int j = j0 + f;
-                float v = kInf;
-                if (j < m) {
-                    const int src = frame_of(fmap, j, ld, A.fault);
-                    v = c < D ? __ldg(xa + (size_t)c * ld + src)
-                              : __ldg(xb + (size_t)(c - D) * ld + src);
-                }
-                tile[c][f] = v;
-            }
+            stage_tile<D, NT, J>(tile, P, j0, tid, A.fault);
             __syncthreads();
-            const int jn = min(J, m - j0);
-            const int ngroups = (jn + 3) >> 2;
-            for (int g = 0; g < ngroups; ++g) {
-                float4 ga[D], gb[D];
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    ga[c] = *reinterpret_cast<const float4*>(&tile[c][4 * g]);
-                    gb[c] = *reinterpret_cast<const float4*>(&tile[D + c][4 * g]);
-                }
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    float da[4], db[4], dz[4];
-                    Marg<D, VARIANT>::four(qa[r], ga, da);
-                    Marg<D, VARIANT>::four(qb[r], gb, db);
-#pragma unroll
-                    for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
-                    const float mn = nsg_min3(dz[0], dz[1], fminf(dz[2], dz[3]));
-                    if (mn < bd[r][KMAX - 1]) {
-#pragma unroll
-                        for (int f = 0; f < 4; ++f) {
-                            if (dz[f] < bd[r][KMAX - 1]) {
-                                list_insert<KMAX>(bd[r], bj[r], dz[f], j0 + 4 * g + f);
-                            }
-                        }
-                    }
-                }
-            }
+            pass1_tile<D, KMAX, R, VARIANT>(&tile[0][0], J, j0, min(J, m - j0), qa, qb, bd, bj);
         }
-
-        // ---- eps from list positions 1..k ---------------------------------------
-        // Position p is slot nsent+p; positions 1..k are slots nsent+1 ..
-        // KMAX-2 and position k+1 is slot KMAX-1. When the k-th distance
-        // equals the (k+1)-th (and is not zero) the reference's choice among
-        // the equal frames depends on its sort; such samples go to the tie
-        // list and ksg_tie_kernel recomputes them.
-        float ea[R], eb[R];
+        float ea[R], eb[R], wk[R], ra[R], rb[R];
+        bool tie[R], mixed[R];
+        eps_and_ties<D, KMAX, R>(A, w, P, qa, qb, qi, bd, bj, ea, eb, tie, wk, ra, rb);
+        bool any_tie = false;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            ea[r] = 0.f;
-            eb[r] = 0.f;
-            const bool valid = qi[r] < w.q1;
-            if (valid && bd[r][KMAX - 2] == bd[r][KMAX - 1] && bd[r][KMAX - 2] > 0.f) {
-                const int slot = atomicAdd(A.tie_count, 1);
-                if (slot < A.tie_cap) {
-                    A.ties[slot] = KsgTie{w.pair, qi[r]};
-                } else {
-                    atomicOr(A.fault, FAULT_TIE_OVERFLOW);
-                }
-            }
-#pragma unroll
-            for (int s = 1; s < KMAX - 1; ++s) {
-                const int j = bj[r][s];
-                if (valid && s > nsent && j >= 0 && j < m) {
-                    const int src = frame_of(fmap, j, ld, A.fault);
-                    ea[r] = fmaxf(ea[r], marginal_at<D>(qa[r], xa, ld, src));
-                    eb[r] = fmaxf(eb[r], marginal_at<D>(qb[r], xb, ld, src));
-                }
-            }
+            mixed[r] = false;
+            any_tie |= tie[r];
         }
+        // warp-uniform: the tie-group check only runs in warps that need it
+        any_tie = __any_sync(0xffffffffu, any_tie);
 
         // ---- pass 2: marginal counts ------------------------------------------
         int ca[R], cb[R];
@@ -281,60 +407,177 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
             const int j0 = t * J;
             if (ntiles > 1) {
                 __syncthreads();
-                for (int idx = tid; idx < 2 * D * J; idx += NT) {
-                    const int c = idx / J;
-                    const int f = idx - c * J;
-                    const int j = j0 + f;
-                    float v = kInf;
-                    if (j < m) {
-                        const int src = frame_of(fmap, j, ld, A.fault);
-                        v = c < D ? __ldg(xa + (size_t)c * ld + src)
-                                  : __ldg(xb + (size_t)(c - D) * ld + src);
-                    }
-                    tile[c][f] = v;
-                }
+                stage_tile<D, NT, J>(tile, P, j0, tid, A.fault);
                 __syncthreads();
             }
-            const int jn = min(J, m - j0);
-            const int ngroups = (jn + 3) >> 2;
-            for (int g = 0; g < ngroups; ++g) {
-                float4 ga[D], gb[D];
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    ga[c] = *reinterpret_cast<const float4*>(&tile[c][4 * g]);
-                    gb[c] = *reinterpret_cast<const float4*>(&tile[D + c][4 * g]);
-                }
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    float da[4], db[4];
-                    Marg<D, VARIANT>::four(qa[r], ga, da);
-                    Marg<D, VARIANT>::four(qb[r], gb, db);
-#pragma unroll
-                    for (int f = 0; f < 4; ++f) {
-                        ca[r] += da[f] <= ea[r] ? 1 : 0;
-                        cb[r] += db[f] <= eb[r] ? 1 : 0;
-                    }
-                }
+            if (any_tie) {
+                pass2_tile<D, R, VARIANT, true>(&tile[0][0], J, min(J, m - j0), qa, qb, ea, eb, ca,
+                                                cb, wk, ra, rb, mixed);
+            } else {
+                pass2_tile<D, R, VARIANT, false>(&tile[0][0], J, min(J, m - j0), qa, qb, ea, eb, ca,
+                                                 cb, wk, ra, rb, mixed);
             }
         }
+        report_ties<R>(A, w, qi, tie, mixed);
+        write_outputs<KMAX, R>(A, w, P, qi, bd, ea, eb, ca, cb);
+    }
+}
 
-        // ---- per-sample outputs -----------------------------------------------
+// Staging by bulk copies (TMA): two shared-memory stages, one elected
+// thread issues one cp.async.bulk per coordinate plane per tile, completing
+// on the stage's mbarrier, and the next-but-one tile is requested as soon as
+// a stage has been read, so copies overlap the distance arithmetic. The
+// copies move whole 16-byte groups; the last < 4 frames of a pair and the
+// +inf padding of its last group are written by threads. Requires row
+// starts 16-byte aligned, a plane stride that is a multiple of 4 and no frame
+// map (the planner checks). Every wait is bounded: when one runs out the
+// kernel records FAULT_WAIT_TIMEOUT, waits (bounded) for the copies it has
+// in flight and returns.
+constexpr unsigned kWaitPolls = 1u << 22;
+
+template <int D, int KMAX, int R, int NT, int J, int VARIANT>
+__global__ void __launch_bounds__(NT) ksg_count_kernel_tma(KsgCountArgs A) {
+    static_assert(J % (4 * 32) == 0, "tile must hold whole float4 groups");
+    constexpr int kStage = 2 * D * J;  // floats per stage
+    extern __shared__ __align__(128) float smem[];
+    __shared__ __align__(8) unsigned long long bars[2];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    const float kInf = __int_as_float(0x7f800000);
+    const uint32_t bar0 = nsg_smem_addr(&bars[0]);
+    const uint32_t bar1 = nsg_smem_addr(&bars[1]);
+    if (tid == 0) {
+        nsg_mbar_init(bar0, 1);
+        nsg_mbar_init(bar1, 1);
+        nsg_fence_mbar_init();
+    }
+    __syncthreads();
+    // phases consumed and copies in flight per stage (same in every thread);
+    // scalars, not arrays, so they stay in registers
+    unsigned phase0 = 0u, phase1 = 0u;
+    int inflight0 = 0, inflight1 = 0;
+
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(A.counter, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= A.nitems) return;
+        const KsgItem w = A.items[item];
+        const KsgPairDesc P = A.pairs[w.pair];
+        const int m = P.m;
+        const int T = (m + J - 1) / J;
+        const int nv = T == 1 ? 1 : 2 * T;  // pass-1 tiles, then pass-2 tiles
+
+        // thread 0: request virtual tile v into stage v & 1
+        auto issue = [&](int v) {
+            const int st = v & 1;
+            const int j0 = (v % T) * J;
+            const int bulk = min(J, m - j0) & ~3;
+            const uint32_t bar = st ? bar1 : bar0;
+            nsg_fence_proxy_async();
+            nsg_mbar_arrive_expect_tx(bar, static_cast<uint32_t>(2 * D * bulk * 4));
+            if (bulk > 0) {
+#pragma unroll
+                for (int c = 0; c < 2 * D; ++c) {
+                    const float* src = (c < D ? P.xa + (size_t)c * P.ld : P.xb + (size_t)(c - D) * P.ld) + j0;
+                    nsg_bulk_load(nsg_smem_addr(smem + st * kStage + c * J), src,
+                                  static_cast<uint32_t>(bulk * 4), bar);
+                }
+            }
+        };
+        if (tid == 0) {
+            issue(0);
+            if (nv > 1) issue(1);
+        }
+        inflight0 += 1;
+        if (nv > 1) inflight1 += 1;
+
+        float qa[R][D], qb[R][D];
+        int qi[R];
+        float bd[R][KMAX];
+        int bj[R][KMAX];
+        load_queries<D, KMAX, R, NT>(A, w, P, tid, qa, qb, qi, bd, bj);
+        float ea[R], eb[R], wk[R], ra[R], rb[R];
+        bool tie[R], mixed[R];
+        bool any_tie = false;
+        int ca[R], cb[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            if (qi[r] < w.q1) {
-                const long long o = P.scratch + qi[r];
-                // counts lie in [k, m-1] for finite inputs; the clamp keeps
-                // non-finite inputs from indexing outside the psi table
-                const int nx = min(max(ca[r] - 1, 0), m);
-                const int ny = min(max(cb[r] - 1, 0), m);
-                A.psum[o] = __fadd_rn(__ldg(A.psi + nx), __ldg(A.psi + ny));
-                if (A.nx) A.nx[o] = nx;
-                if (A.ny) A.ny[o] = ny;
-                if (A.eps_x) A.eps_x[o] = ea[r];
-                if (A.eps_y) A.eps_y[o] = eb[r];
-                if (A.kdist) A.kdist[o] = bd[r][KMAX - 2];
+            ca[r] = 0;
+            cb[r] = 0;
+            mixed[r] = false;
+        }
+
+        for (int v = 0; v < nv; ++v) {
+            const int st = v & 1;
+            const int j0 = (v % T) * J;
+            const int jn = min(J, m - j0);
+            const unsigned ph = st ? phase1 : phase0;
+            const bool ok = nsg_mbar_wait(st ? bar1 : bar0, ph & 1u, kWaitPolls);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicOr(A.fault, FAULT_WAIT_TIMEOUT);
+                // leave no copy in flight into shared memory we give up
+                for (int u = 0; u < inflight0; ++u) nsg_mbar_wait(bar0, (phase0 + u) & 1u, kWaitPolls);
+                for (int u = 0; u < inflight1; ++u) nsg_mbar_wait(bar1, (phase1 + u) & 1u, kWaitPolls);
+                return;
+            }
+            if (st) {
+                phase1 += 1;
+                inflight1 -= 1;
+            } else {
+                phase0 += 1;
+                inflight0 -= 1;
+            }
+            float* tile = smem + st * kStage;
+            const int bulk = jn & ~3;
+            if (bulk != jn || (jn & 3)) {
+                // tail frames and the +inf padding of the last group
+                const int tail_end = (jn + 3) & ~3;
+                for (int idx = tid; idx < 2 * D * 4; idx += NT) {
+                    const int c = idx >> 2;
+                    const int f = bulk + (idx & 3);
+                    if (f < tail_end) {
+                        float val = kInf;
+                        if (f < jn) {
+                            val = c < D ? __ldg(P.xa + (size_t)c * P.ld + j0 + f)
+                                        : __ldg(P.xb + (size_t)(c - D) * P.ld + j0 + f);
+                        }
+                        tile[c * J + f] = val;
+                    }
+                }
+                // order these generic-proxy writes before a later bulk copy
+                // into the same stage
+                nsg_fence_proxy_async();
+                __syncthreads();
+            }
+            if (v < T || T == 1) {
+                pass1_tile<D, KMAX, R, VARIANT>(tile, J, j0, jn, qa, qb, bd, bj);
+                if (v == T - 1) {
+                    eps_and_ties<D, KMAX, R>(A, w, P, qa, qb, qi, bd, bj, ea, eb, tie, wk, ra, rb);
+#pragma unroll
+                    for (int r = 0; r < R; ++r) any_tie |= tie[r];
+                    any_tie = __any_sync(0xffffffffu, any_tie);
+                }
+            }
+            if (v >= T || T == 1) {
+                if (any_tie) {
+                    pass2_tile<D, R, VARIANT, true>(tile, J, jn, qa, qb, ea, eb, ca, cb, wk, ra, rb,
+                                                    mixed);
+                } else {
+                    pass2_tile<D, R, VARIANT, false>(tile, J, jn, qa, qb, ea, eb, ca, cb, wk, ra, rb,
+                                                     mixed);
+                }
+            }
+            __syncthreads();  // stage st fully read
+            if (v + 2 < nv) {
+                if (tid == 0) issue(v + 2);
+                if (st) inflight1 += 1;
+                else inflight0 += 1;
             }
         }
+        report_ties<R>(A, w, qi, tie, mixed);
+        write_outputs<KMAX, R>(A, w, P, qi, bd, ea, eb, ca, cb);
     }
 }
 

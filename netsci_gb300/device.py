@@ -125,9 +125,11 @@ class KsgPlan:
 
     @property
     def shape(self) -> dict:
-        v = [ctypes.c_int() for _ in range(4)]
-        call("nsg_ksg_plan_shape", self._h, *(ctypes.byref(x) for x in v))
-        return dict(threads=v[0].value, r=v[1].value, frames=v[2].value, variant=v[3].value)
+        v = [ctypes.c_int() for _ in range(5)]
+        call("nsg_ksg_plan_shape", self._h, *(ctypes.byref(x) for x in v[:4]))
+        call("nsg_ksg_plan_staging", self._h, ctypes.byref(v[4]))
+        return dict(threads=v[0].value, r=v[1].value, frames=v[2].value, variant=v[3].value,
+                    staging="bulk-copy" if v[4].value else "loads")
 
     def count_ms(self) -> float:
         """Device time (ms) of the count kernels in the last run."""
@@ -150,6 +152,11 @@ class KsgPlan:
 def set_ksg_shape(threads: int = 0, r: int = 0, frames: int = 0, variant: int = -1) -> None:
     """Force a KSG tile shape for later plans (threads=0: automatic)."""
     call("nsg_ksg_set_shape", int(threads), int(r), int(frames), int(variant))
+
+
+def set_ksg_staging(staging: int = -1) -> None:
+    """Tile staging for later plans: 1 bulk copies (TMA), 0 plain loads, -1 auto."""
+    call("nsg_ksg_set_staging", int(staging))
 
 
 def apsp_lengths(A: torch.Tensor, max_path_length: int, H: torch.Tensor | None = None,

@@ -307,3 +307,76 @@ def test_autotuned_plan_same_results_and_cached(tmp_path, monkeypatch):
     assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
     sh = tuned.shape
     assert sh["threads"] in (64, 128, 256, 512) and sh["r"] in (1, 2)
+
+
+TMA_SHAPES = [(256, 1, 1024), (128, 1, 1024), (512, 1, 1024), (256, 1, 512)]
+
+
+@pytest.mark.parametrize("d,k", [(1, 4), (2, 6), (3, 6)])
+def test_bulk_copy_staging_agrees(oracle_mod, d, k):
+    """The bulk-copy (TMA) staged kernels against the oracle at sample counts
+    that give one tile, several tiles and ragged tails (m mod 4 = 0..3)."""
+    from netsci_gb300 import device
+    rng = np.random.default_rng(40 + d)
+    try:
+        for n in (9, 130, 1023, 1026, 2049, 3075):
+            xa = rng.standard_normal(d * n).astype(np.float32)
+            xb = (0.6 * xa + rng.standard_normal(d * n)).astype(np.float32)
+            mi, det = oracle_mod.mi_pair(xa, xb, n, k, d, detail=True)
+            for shape in TMA_SHAPES:
+                device.set_ksg_shape(*shape)
+                device.set_ksg_staging(1)
+                out = _mi_device(xa, xb, n, k, d)
+                assert float(out["mi"].item()) == mi, (n, shape)
+                for key in ("n_x", "n_y", "eps_x", "eps_y"):
+                    assert np.array_equal(out[key].cpu().numpy(), det[key]), (n, shape, key)
+    finally:
+        device.set_ksg_staging(-1)
+        device.set_ksg_shape(0)
+
+
+def test_bulk_copy_plan_many_pairs(oracle_mod):
+    """A multi-pair plan with bulk-copy staging, replayed through a graph."""
+    from netsci_gb300 import device, synthetic
+    X, _ = synthetic.protein_trajectory(9, 1500, seed=12)
+    Xd, m = device.pack_trajectory(X, 3)
+    ab = synthetic.all_pairs(9)
+    pairs = device.make_pairs(Xd, m, ab)
+    expect = oracle_mod.pairs(X, m, 3, ab, 6, gc=False, threads=8)
+    try:
+        device.set_ksg_staging(1)
+        mi = torch.empty(len(pairs), device="cuda")
+        plan = device.KsgPlan(pairs, 6, 3, mi=mi, graph=True)
+        assert plan.shape["staging"] == "bulk-copy"
+        for _ in range(2):
+            plan.run()
+            torch.cuda.synchronize()
+            plan.check()
+            assert np.array_equal(mi.cpu().numpy(), expect)
+    finally:
+        device.set_ksg_staging(-1)
+
+
+def test_bootstrap_duplicates_and_real_ties(oracle_mod):
+    """Bootstrap resampling makes copies of frames (ties that cannot change
+    eps, not listed) and a coarse grid makes genuine ties (listed and
+    resolved in the reference's sort order); both together, on enough pairs
+    that listing every tied sample would overflow the tie list."""
+    from netsci_gb300 import device
+    rng = np.random.default_rng(17)
+    N, m, k = 8, 2500, 6
+    X = (np.round(rng.standard_normal((N, 3 * m)) * 6) / 6).astype(np.float32)
+    X[1::2] = rng.standard_normal((N // 2, 3 * m)).astype(np.float32)
+    Xd, mm = device.pack_trajectory(X, 3)
+    idx = rng.integers(0, m, size=m).astype(np.int32)
+    fmap = torch.from_numpy(idx).cuda()
+    ab = np.array([[a, b] for a in range(N) for b in range(N) if a != b], np.int32)
+    pairs = device.make_pairs(Xd, mm, ab, fmap=fmap, m_samples=m)
+    mi = torch.empty(len(pairs), device="cuda")
+    plan = device.KsgPlan(pairs, k, 3, mi=mi)
+    plan.run()
+    torch.cuda.synchronize()
+    plan.check()
+    Xr = X.reshape(N, 3, m)[:, :, idx].reshape(N, 3 * m)
+    expect = oracle_mod.pairs(Xr, m, 3, ab, k, gc=False, threads=8)
+    assert np.array_equal(mi.cpu().numpy(), expect)
