@@ -188,6 +188,12 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
             variant_ = g_forced_variant;
         }
     }
+    int staging = opt.staging;
+    if (staging < 0) {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        staging = g_forced_staging;
+    }
+    const bool bulk_ok = ksg_bulk_copy_ok(pairs);
     int tuned_staging = -1;
     if (!shape_.threads && opt.autotune && npairs > 0) {
         const KsgTuned t = ksg_autotune(pairs, k, d);
@@ -196,7 +202,8 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         tuned_staging = t.staging;
     }
     if (shape_.threads) {
-        if (!ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_)) {
+        if (!ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_, 0) &&
+            !ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_, 1)) {
             fail(NSG_ERR_UNSUPPORTED, "requested KSG shape is not instantiated for this d/k");
         }
     } else {
@@ -208,7 +215,9 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         const int nc = std::min(32, ksg_list_entries(d, kmax_, cand, 32));
         std::vector<const KsgKernelEntry*> pref;
         for (int i = 0; i < nc; ++i) {
-            if (cand[i]->variant == cand[0]->variant && !cand[i]->tma) pref.push_back(cand[i]);
+            if (cand[i]->variant == cand[0]->variant && cand[i]->tma == (staging == 1 && bulk_ok ? 1 : 0)) {
+                pref.push_back(cand[i]);
+            }
         }
         std::stable_sort(pref.begin(), pref.end(), [](const KsgKernelEntry* a, const KsgKernelEntry* b) {
             if (a->r != b->r) return a->r < b->r;
@@ -230,14 +239,8 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
     }
     // staging: plain loads unless the plan option, the override or the
     // autotuner asks for bulk copies (which need aligned rows and no frame map)
-    int staging = opt.staging;
-    if (staging < 0) {
-        std::lock_guard<std::mutex> lk(g_shape_mu);
-        staging = g_forced_staging;
-    }
     if (staging < 0) staging = tuned_staging;
     if (staging < 0) staging = 0;
-    const bool bulk_ok = ksg_bulk_copy_ok(pairs);
     const KsgKernelEntry* entry = nullptr;
     if (staging != 0 && bulk_ok) {
         entry = ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_, 1);
@@ -247,7 +250,10 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
                                           : "bulk-copy staging needs aligned rows and no frame map");
     }
     if (!entry) entry = ksg_find_entry(d, kmax_, shape_.threads, shape_.r, shape_.frames, variant_, 0);
-    if (!entry) fail(NSG_ERR_UNSUPPORTED, "no KSG kernel instantiated for this shape");
+    if (!entry) {
+        fail(NSG_ERR_UNSUPPORTED, bulk_ok ? "KSG shape only has a bulk-copy kernel; staging was set to loads"
+                                          : "KSG shape only has a bulk-copy kernel, which needs aligned rows and no frame map");
+    }
     entry_ = entry;
     variant_ = entry->variant;
     const int qc = shape_.threads * shape_.r;
