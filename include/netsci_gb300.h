@@ -143,6 +143,15 @@ int nsg_recover_single_shortest_path(nsg_cuarray* paths, int max_path_length, in
                                      int** path, int* len);
 /* netcalc/include/psi.h:160-163 (generatePsi, table of n+1 floats) */
 int nsg_generate_psi(nsg_cuarray* psi, int n);
+/* netcalc/include/math_utils.h:22-95 (mean, meanGpu, standardDeviation,
+ * standardDeviationGpu): row means / population standard deviations of a
+ * row-major matrix; the platform calls re-initialise u (and sigma) to
+ * 1 x (size/n) and compute only for platform 0, as the reference.          */
+int nsg_mean(nsg_cuarray* a, nsg_cuarray* u, int m, int n, int platform);
+int nsg_mean_gpu(nsg_cuarray* a, nsg_cuarray* u, int m, int n);
+int nsg_standard_deviation(nsg_cuarray* a, nsg_cuarray* u, nsg_cuarray* sigma, int m, int n,
+                           int platform);
+int nsg_standard_deviation_gpu(nsg_cuarray* a, nsg_cuarray* u, nsg_cuarray* sigma, int m, int n);
 
 /* ---- 3. device-pointer entry points -------------------------------------- */
 
@@ -247,6 +256,10 @@ int nsg_apsp_paths_device(const float* A, float* H, int* paths, int n, int max_p
  * (netcalc/src/hedetniemi_gpu.cu:10-26); mode 1 = -ln(r) with +inf for
  * r <= 0. Diagonal 0 in both.                                             */
 int nsg_corr_to_adjacency_device(const float* C, float* A, int n, int mode, void* stream);
+/* Row means (and, with sigma non-null, population standard deviations) of
+ * a device row-major m x n matrix into device u[m], sigma[m]; the
+ * summation order of netcalc/src/math_utils_gpu.cu:22-158.                 */
+int nsg_row_stats_device(const float* a, float* u, float* sigma, int m, int n, void* stream);
 
 /* ---- 4. serving: continuous batching of MI / GC / APSP jobs ------------- */
 /* A request loop with no reference counterpart (the reference serves one

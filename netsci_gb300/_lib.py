@@ -96,6 +96,10 @@ _SIGNATURES = {
     "nsg_correlation_to_adjacency": (c_int, [c_void_p, c_void_p, c_int, c_int]),
     "nsg_recover_single_shortest_path": (c_int, [c_void_p, c_int, c_int, c_int, PP_int, P_int]),
     "nsg_generate_psi": (c_int, [c_void_p, c_int]),
+    "nsg_mean": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int]),
+    "nsg_mean_gpu": (c_int, [c_void_p, c_void_p, c_int, c_int]),
+    "nsg_standard_deviation": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int]),
+    "nsg_standard_deviation_gpu": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int]),
     "nsg_ksg_pairs_device": (c_int, [ctypes.POINTER(KsgPair), c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "nsg_ksg_pair_detail_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "nsg_ksg_pair_noalloc_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
@@ -122,6 +126,7 @@ _SIGNATURES = {
     "nsg_apsp_lengths_device": (c_int, [c_void_p, c_void_p, c_int, c_int, P_int, c_void_p]),
     "nsg_apsp_paths_device": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_float, c_void_p]),
     "nsg_corr_to_adjacency_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    "nsg_row_stats_device": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
 }
 
 _LIB = None

@@ -25,7 +25,8 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["ksg_d1.cu", "ksg_d2.cu", "ksg_d3.cu", "ksg.cu", "ksg_tie.cu", "ksg_noalloc.cu", "apsp.cu"]
+CU_SOURCES = ["ksg_d1.cu", "ksg_d2.cu", "ksg_d3.cu", "ksg.cu", "ksg_tie.cu", "ksg_noalloc.cu", "apsp.cu",
+              "rowstats.cu"]
 CPP_SOURCES = ["cuarray.cpp", "npy.cpp", "engine.cpp", "ksg_cpu.cpp", "netcalc.cpp", "serve.cpp", "capi.cpp"]
 
 

@@ -20,7 +20,9 @@
 #include "netcalc/generalized_correlation.h"
 #include "netcalc/hedetniemi.h"
 #include "netcalc/mutual_information.h"
+#include "netcalc/math_utils.h"
 #include "netcalc/psi.h"
+#include "rowstats.h"
 #include "netsci_gb300.h"
 
 struct nsg_cuarray {
@@ -382,6 +384,28 @@ int nsg_generate_psi(nsg_cuarray* psi, int n) {
     return guarded([&] { generatePsi(as<float>(psi, "psi"), n); });
 }
 
+int nsg_mean(nsg_cuarray* a, nsg_cuarray* u, int m, int n, int platform) {
+    return guarded([&] { mean(as<float>(a, "a"), as<float>(u, "u"), m, n, platform); });
+}
+
+int nsg_mean_gpu(nsg_cuarray* a, nsg_cuarray* u, int m, int n) {
+    return guarded([&] { meanGpu(as<float>(a, "a"), as<float>(u, "u"), m, n); });
+}
+
+int nsg_standard_deviation(nsg_cuarray* a, nsg_cuarray* u, nsg_cuarray* sigma, int m, int n,
+                           int platform) {
+    return guarded([&] {
+        standardDeviation(as<float>(a, "a"), as<float>(u, "u"), as<float>(sigma, "sigma"), m, n,
+                          platform);
+    });
+}
+
+int nsg_standard_deviation_gpu(nsg_cuarray* a, nsg_cuarray* u, nsg_cuarray* sigma, int m, int n) {
+    return guarded([&] {
+        standardDeviationGpu(as<float>(a, "a"), as<float>(u, "u"), as<float>(sigma, "sigma"), m, n);
+    });
+}
+
 // ---- device-pointer entry points ----------------------------------------------
 int nsg_ksg_pairs_device(const nsg_ksg_pair* pairs, int npairs, int k, int d, float* mi,
                          float* gc, float* w, void* stream) {
@@ -531,6 +555,13 @@ int nsg_corr_to_adjacency_device(const float* C, float* A, int n, int mode, void
     return guarded([&] {
         if (mode != 0 && mode != 1) nsg::invalid("mode must be 0 (1/r) or 1 (-ln r)");
         nsg::corr_to_adjacency(C, A, n, mode, stream_of(stream));
+    });
+}
+
+int nsg_row_stats_device(const float* a, float* u, float* sigma, int m, int n, void* stream) {
+    return guarded([&] {
+        if (m > 0 && (!a || !u)) nsg::invalid("a and u must be device pointers");
+        nsg::row_stats(a, u, sigma, m, n, stream_of(stream));
     });
 }
 

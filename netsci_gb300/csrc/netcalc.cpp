@@ -21,7 +21,9 @@
 #include "netcalc/generalized_correlation.h"
 #include "netcalc/hedetniemi.h"
 #include "netcalc/mutual_information.h"
+#include "netcalc/math_utils.h"
 #include "netcalc/psi.h"
+#include "rowstats.h"
 
 namespace nsg {
 namespace {
@@ -357,4 +359,57 @@ void generatePsi(CuArray<float>* psi, int n) {
         const float inv = static_cast<float>(1.0 / static_cast<float>(i));
         psi->set(psi->get(0, i) + inv, 0, i + 1);
     }
+}
+
+// ---- row statistics (netcalc/src/math_utils.cpp:6-36, math_utils_gpu.cu:160-198) ----
+namespace {
+// Device copy of a (made from the host copy when a has none), u and sigma
+// computed on the device and copied back to their host buffers.
+void row_stats_cuarray(CuArray<float>* a, CuArray<float>* u, CuArray<float>* sigma, int m, int n) {
+    if (!a || !u) nsg::invalid("a and u must be CuArrays");
+    if (m < 0 || n < 1) nsg::invalid("row statistics need m >= 0 and n >= 1");
+    if (static_cast<long long>(m) * n > a->size()) nsg::invalid("a holds fewer than m*n values");
+    if (u->size() < m || (sigma && sigma->size() < m)) {
+        nsg::invalid("u and sigma must hold m values (initialise them first)");
+    }
+    if (m == 0) return;
+    if (!a->allocatedDevice()) {
+        if (a->allocateDevice() || a->toDevice()) nsg::fail(NSG_ERR_CUDA, "cannot copy a to the device");
+    }
+    if (!u->allocatedDevice() && u->allocateDevice()) nsg::fail(NSG_ERR_CUDA, "cannot allocate u");
+    if (sigma && !sigma->allocatedDevice() && sigma->allocateDevice()) {
+        nsg::fail(NSG_ERR_CUDA, "cannot allocate sigma");
+    }
+    nsg::row_stats(a->device(), u->device(), sigma ? sigma->device() : nullptr, m, n, nullptr);
+    NSG_CUDA(cudaDeviceSynchronize());
+    if (u->toHost() || (sigma && sigma->toHost())) nsg::fail(NSG_ERR_CUDA, "cannot copy results back");
+}
+}  // namespace
+
+void mean(CuArray<float>* a, CuArray<float>* u, int m, int n, int platform) {
+    if (!a || !u) nsg::invalid("a and u must be CuArrays");
+    if (n < 1) nsg::invalid("n must be >= 1");
+    m = a->size() / n;
+    u->init(1, m);
+    if (platform == 0) meanGpu(a, u, m, n);
+}
+
+void meanGpu(CuArray<float>* a, CuArray<float>* u, int m, int n) {
+    row_stats_cuarray(a, u, nullptr, m, n);
+}
+
+void standardDeviation(CuArray<float>* a, CuArray<float>* u, CuArray<float>* sigma, int m, int n,
+                       int platform) {
+    if (!a || !u || !sigma) nsg::invalid("a, u and sigma must be CuArrays");
+    if (n < 1) nsg::invalid("n must be >= 1");
+    m = a->size() / n;
+    u->init(1, m);
+    sigma->init(1, m);
+    if (platform == 0) standardDeviationGpu(a, u, sigma, m, n);
+}
+
+void standardDeviationGpu(CuArray<float>* a, CuArray<float>* u, CuArray<float>* sigma, int m,
+                          int n) {
+    if (!sigma) nsg::invalid("sigma must be a CuArray");
+    row_stats_cuarray(a, u, sigma, m, n);
 }

@@ -117,6 +117,26 @@ def correlationToAdjacency(A, C, n, platform=GPU_PLATFORM):
     call("nsg_correlation_to_adjacency", A.handle, C.handle, int(n), int(platform))
 
 
+def mean(a, u, m, n, platform=GPU_PLATFORM):
+    """Row means of a (rows of n values) into u, re-initialised to 1 x (size/n);
+    computed for the GPU platform only, as the reference."""
+    call("nsg_mean", a.handle, u.handle, int(m), int(n), int(platform))
+
+
+def meanGpu(a, u, m, n):
+    call("nsg_mean_gpu", a.handle, u.handle, int(m), int(n))
+
+
+def standardDeviation(a, u, sigma, m, n, platform=GPU_PLATFORM):
+    """Row means into u and population standard deviations into sigma."""
+    call("nsg_standard_deviation", a.handle, u.handle, sigma.handle, int(m), int(n),
+         int(platform))
+
+
+def standardDeviationGpu(a, u, sigma, m, n):
+    call("nsg_standard_deviation_gpu", a.handle, u.handle, sigma.handle, int(m), int(n))
+
+
 def recoverSingleShortestPath(paths, maxPathLength, i, j) -> np.ndarray:
     """Node sequence from i to j as an int32 numpy array."""
     p = ctypes.POINTER(ctypes.c_int)()
@@ -226,6 +246,7 @@ __all__ = [
     "generalizedCorrelationGpu", "generalizedCorrelationCpu", "hedetniemiAllShortestPaths",
     "hedetniemiAllShortestPathsGpu", "hedetniemiAllShortestPathLengths",
     "hedetniemiAllShortestPathLengthsGpu", "correlationToAdjacency", "recoverSingleShortestPath",
+    "mean", "meanGpu", "standardDeviation", "standardDeviationGpu",
     "GPU_PLATFORM", "CPU_PLATFORM", "generateRestartAbFromCheckpointFile", "generatePsi",
     "MutualInformationSettings", "GeneralizedCorrelationSettings", "FloatCuArray", "IntCuArray",
 ]

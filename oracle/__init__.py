@@ -180,3 +180,40 @@ def corr_to_neglog_adj(C):
     A = np.zeros_like(C)
     lib().oracle_corr_to_neglog_adj(C.ravel(), A.ravel(), C.shape[0])
     return A
+
+
+def _fold_1024(p: np.ndarray) -> np.float32:
+    """Pairwise fold p[t] += p[t + s], s = 512 .. 1, in float32
+    (netcalc/src/math_utils_gpu.cu:10-20,36-60)."""
+    p = p.copy()
+    s = 512
+    while s >= 1:
+        p[:s] = p[:s] + p[s:2 * s]
+        s >>= 1
+    return p[0]
+
+
+def row_stats(a, n: int):
+    """Row means and population standard deviations of a (rows of n values)
+    in the reference kernels' summation order: thread slot t of 1024 sums
+    a[t], a[t + 1024], ... sequentially in float32, then the 1024 partial sums
+    are folded pairwise (netcalc/src/math_utils_gpu.cu:22-158). The square is
+    d * d (the reference writes powf(d, 2.0))."""
+    a = _c(a, np.float32).ravel()
+    m = a.size // n
+    a = a[:m * n].reshape(m, n)
+    nf = np.float32(n)
+    u = np.zeros(m, np.float32)
+    sigma = np.zeros(m, np.float32)
+    for r in range(m):
+        p = np.zeros(1024, np.float32)
+        for j0 in range(0, n, 1024):
+            chunk = a[r, j0:j0 + 1024]
+            p[:chunk.size] = p[:chunk.size] + chunk
+        u[r] = np.float32(_fold_1024(p) / nf)
+        q = np.zeros(1024, np.float32)
+        for j0 in range(0, n, 1024):
+            dv = a[r, j0:j0 + 1024] - u[r]
+            q[:dv.size] = q[:dv.size] + dv * dv
+        sigma[r] = np.sqrt(np.float32(_fold_1024(q) / nf), dtype=np.float32)
+    return u, sigma
