@@ -292,6 +292,56 @@ int nsg_server_job_info(nsg_server* s, long long job, int* state, double* submit
 int nsg_server_stats(nsg_server* s, long long* jobs_done, long long* pairs_done,
                      long long* ticks, size_t* peak_bytes);
 
+/* ---- 5. netchem: trajectory -> node coordinates --------------------------- */
+/* netchem::Network (netchem/include/network.h:19-172) over an opaque handle.
+ * nsg_network_init replaces Network::init (netchem/src/network.cpp:29-75):
+ * PDB ATOM records grouped into nodes by residue tag, DCD frames first,
+ * first + stride, ..., <= last (last == -1: the file's last frame), node
+ * mass-weighted centres computed on the device. Atom and node fields are
+ * those of netchem/include/atom.h:57-189 and node.h:39-88.                  */
+typedef struct nsg_network nsg_network;
+typedef struct nsg_atom_info {
+    int index, serial, residue_id;
+    float occupancy, temperature_factor, mass;
+    unsigned int hash;
+    char name[8], element[4], residue_name[8], chain_id[4], segment_id[8], tag[40];
+} nsg_atom_info;
+typedef struct nsg_node_info {
+    int index, num_atoms;
+    float total_mass;
+    unsigned int hash;
+    char tag[40];
+} nsg_node_info;
+int nsg_network_create(nsg_network** out);
+int nsg_network_destroy(nsg_network* net);
+int nsg_network_init(nsg_network* net, const char* trajectory_file, const char* topology_file,
+                     int first_frame, int last_frame, int stride);
+/* Network::parsePdb (netchem/src/network.cpp:258-278): appends the file's
+ * ATOM records to the network's atoms (host only; init() calls it).        */
+int nsg_network_parse_pdb(nsg_network* net, const char* topology_file);
+int nsg_network_num_nodes(nsg_network* net, int* n);
+int nsg_network_num_frames(nsg_network* net, int* m);
+int nsg_network_num_atoms(nsg_network* net, int* n);
+/* Copies Network::nodeCoordinates() (N x 3m) into the CuArray `out`. */
+int nsg_network_node_coordinates(nsg_network* net, nsg_cuarray* out);
+/* Network::nodeCoordinates(file): node coordinates from a .npy file. */
+int nsg_network_load_node_coordinates(nsg_network* net, const char* npy_file);
+int nsg_network_node(nsg_network* net, int node, nsg_node_info* out);
+/* Atom indices of a node, in index order; *count = number of atoms (at most
+ * cap are written).                                                        */
+int nsg_network_node_atoms(nsg_network* net, int node, int* atoms, int cap, int* count);
+int nsg_network_atom(nsg_network* net, int atom, nsg_atom_info* out);
+int nsg_network_node_from_atom(nsg_network* net, int atom, int* node);
+/* Device-resident node coordinates (valid until the next init or destroy):
+ * row n at *X + n*3*(*ld), planes x, y, z of *ld floats, +inf past m. The
+ * rows can be passed as nsg_ksg_pair.xa / .xb with d = 3.                  */
+int nsg_network_device_coordinates(nsg_network* net, const float** X, int* ld);
+/* DCD frames on the host (the reader under nsg_network_init): atom and
+ * frame counts, and frames first, first + stride, ... (count of them) into
+ * xyz[f][c][atom] (c = x, y, z). netchem/src/dcd/dcd.cpp:775-940.          */
+int nsg_dcd_info(const char* path, int* natoms, int* nsets);
+int nsg_dcd_read(const char* path, int first, int count, int stride, float* xyz);
+
 #ifdef __cplusplus
 }
 #endif

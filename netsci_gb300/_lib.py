@@ -46,6 +46,23 @@ class KsgPair(ctypes.Structure):
                 ("m", c_int)]
 
 
+class AtomInfo(ctypes.Structure):
+    """nsg_atom_info."""
+
+    _fields_ = [("index", c_int), ("serial", c_int), ("residue_id", c_int),
+                ("occupancy", c_float), ("temperature_factor", c_float), ("mass", c_float),
+                ("hash", ctypes.c_uint), ("name", ctypes.c_char * 8), ("element", ctypes.c_char * 4),
+                ("residue_name", ctypes.c_char * 8), ("chain_id", ctypes.c_char * 4),
+                ("segment_id", ctypes.c_char * 8), ("tag", ctypes.c_char * 40)]
+
+
+class NodeInfo(ctypes.Structure):
+    """nsg_node_info."""
+
+    _fields_ = [("index", c_int), ("num_atoms", c_int), ("total_mass", c_float),
+                ("hash", ctypes.c_uint), ("tag", ctypes.c_char * 40)]
+
+
 class NsgError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"[nsg status {status}] {message}")
@@ -127,6 +144,22 @@ _SIGNATURES = {
     "nsg_apsp_paths_device": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_float, c_void_p]),
     "nsg_corr_to_adjacency_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p]),
     "nsg_row_stats_device": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    "nsg_network_create": (c_int, [PP_void]),
+    "nsg_network_destroy": (c_int, [c_void_p]),
+    "nsg_network_init": (c_int, [c_void_p, c_char_p, c_char_p, c_int, c_int, c_int]),
+    "nsg_network_parse_pdb": (c_int, [c_void_p, c_char_p]),
+    "nsg_network_num_nodes": (c_int, [c_void_p, P_int]),
+    "nsg_network_num_frames": (c_int, [c_void_p, P_int]),
+    "nsg_network_num_atoms": (c_int, [c_void_p, P_int]),
+    "nsg_network_node_coordinates": (c_int, [c_void_p, c_void_p]),
+    "nsg_network_load_node_coordinates": (c_int, [c_void_p, c_char_p]),
+    "nsg_network_node": (c_int, [c_void_p, c_int, ctypes.POINTER(NodeInfo)]),
+    "nsg_network_node_atoms": (c_int, [c_void_p, c_int, P_int, c_int, P_int]),
+    "nsg_network_atom": (c_int, [c_void_p, c_int, ctypes.POINTER(AtomInfo)]),
+    "nsg_network_node_from_atom": (c_int, [c_void_p, c_int, P_int]),
+    "nsg_network_device_coordinates": (c_int, [c_void_p, PP_void, P_int]),
+    "nsg_dcd_info": (c_int, [c_char_p, P_int, P_int]),
+    "nsg_dcd_read": (c_int, [c_char_p, c_int, c_int, c_int, c_void_p]),
 }
 
 _LIB = None

@@ -22,6 +22,8 @@
 #include "netcalc/mutual_information.h"
 #include "netcalc/math_utils.h"
 #include "netcalc/psi.h"
+#include "netchem/network.h"
+#include "dcd.h"
 #include "rowstats.h"
 #include "netsci_gb300.h"
 
@@ -629,3 +631,166 @@ int nsg_server_stats(nsg_server* s, long long* jobs_done, long long* pairs_done,
 }
 
 }  // extern "C"
+
+// ---- netchem -----------------------------------------------------------------
+struct nsg_network {
+    Network net;
+};
+
+namespace {
+Network& net_of(nsg_network* h) {
+    if (!h) nsg::invalid("network is null");
+    return h->net;
+}
+
+template <size_t N>
+void put_str(char (&dst)[N], const std::string& s) {
+    std::memset(dst, 0, N);
+    std::memcpy(dst, s.data(), std::min(N - 1, s.size()));
+}
+}  // namespace
+
+int nsg_network_create(nsg_network** out) {
+    return guarded([&] {
+        if (!out) nsg::invalid("out is null");
+        *out = new nsg_network();
+    });
+}
+
+int nsg_network_destroy(nsg_network* net) {
+    return guarded([&] { delete net; });
+}
+
+int nsg_network_init(nsg_network* net, const char* trajectory_file, const char* topology_file,
+                     int first_frame, int last_frame, int stride) {
+    return guarded([&] {
+        if (!trajectory_file || !topology_file) nsg::invalid("file name is null");
+        net_of(net).init(trajectory_file, topology_file, first_frame, last_frame, stride);
+    });
+}
+
+int nsg_network_parse_pdb(nsg_network* net, const char* topology_file) {
+    return guarded([&] {
+        if (!topology_file) nsg::invalid("file name is null");
+        net_of(net).parsePdb(topology_file);
+    });
+}
+
+int nsg_network_num_nodes(nsg_network* net, int* n) {
+    return guarded([&] { *n = net_of(net).numNodes(); });
+}
+
+int nsg_network_num_frames(nsg_network* net, int* m) {
+    return guarded([&] { *m = net_of(net).numFrames(); });
+}
+
+int nsg_network_num_atoms(nsg_network* net, int* n) {
+    return guarded([&] { *n = net_of(net).atoms()->numAtoms(); });
+}
+
+int nsg_network_node_coordinates(nsg_network* net, nsg_cuarray* out) {
+    return guarded([&] {
+        CuArray<float>* src = net_of(net).nodeCoordinates();
+        CuArray<float>* dst = as<float>(out, "out");
+        if (src->size() == 0 || !src->host()) {
+            dst->init(0, 0);
+            return;
+        }
+        dst->init(src->host(), src->m(), src->n());
+    });
+}
+
+int nsg_network_load_node_coordinates(nsg_network* net, const char* npy_file) {
+    return guarded([&] {
+        if (!npy_file) nsg::invalid("file name is null");
+        net_of(net).nodeCoordinates(npy_file);
+    });
+}
+
+int nsg_network_node(nsg_network* net, int node, nsg_node_info* out) {
+    return guarded([&] {
+        Network& n = net_of(net);
+        if (node < 0 || node >= static_cast<int>(n.nodes().size())) nsg::invalid("node index out of range");
+        Node* p = n.nodes()[node];
+        out->index = static_cast<int>(p->index());
+        out->num_atoms = static_cast<int>(p->numAtoms());
+        out->total_mass = p->totalMass();
+        out->hash = p->hash();
+        put_str(out->tag, p->tag());
+    });
+}
+
+int nsg_network_node_atoms(nsg_network* net, int node, int* atoms, int cap, int* count) {
+    return guarded([&] {
+        Network& n = net_of(net);
+        if (node < 0 || node >= static_cast<int>(n.nodes().size())) nsg::invalid("node index out of range");
+        const std::vector<Atom*> a = n.nodes()[node]->atoms();
+        *count = static_cast<int>(a.size());
+        for (int i = 0; i < *count && i < cap; ++i) atoms[i] = a[i]->index();
+    });
+}
+
+int nsg_network_atom(nsg_network* net, int atom, nsg_atom_info* out) {
+    return guarded([&] {
+        Network& n = net_of(net);
+        if (atom < 0 || atom >= n.atoms()->numAtoms()) nsg::invalid("atom index out of range");
+        Atom* a = n.atoms()->at(atom);
+        out->index = a->index();
+        out->serial = a->serial();
+        out->residue_id = a->residueId();
+        out->occupancy = a->occupancy();
+        out->temperature_factor = a->temperatureFactor();
+        out->mass = a->mass();
+        out->hash = a->hash();
+        put_str(out->name, a->name());
+        put_str(out->element, a->element());
+        put_str(out->residue_name, a->residueName());
+        put_str(out->chain_id, a->chainId());
+        put_str(out->segment_id, a->segmentId());
+        put_str(out->tag, a->tag());
+    });
+}
+
+int nsg_network_node_from_atom(nsg_network* net, int atom, int* node) {
+    return guarded([&] {
+        Network& n = net_of(net);
+        if (atom < 0 || atom >= n.atoms()->numAtoms()) nsg::invalid("atom index out of range");
+        *node = static_cast<int>(n.nodeFromAtomIndex(atom)->index());
+    });
+}
+
+int nsg_network_device_coordinates(nsg_network* net, const float** X, int* ld) {
+    return guarded([&] {
+        Network& n = net_of(net);
+        *X = n.deviceCoordinates();
+        *ld = n.deviceLd();
+    });
+}
+
+int nsg_dcd_info(const char* path, int* natoms, int* nsets) {
+    return guarded([&] {
+        if (!path) nsg::invalid("path is null");
+        nsg::DcdFile f(path);
+        *natoms = f.info().natoms;
+        *nsets = f.info().nsets;
+    });
+}
+
+int nsg_dcd_read(const char* path, int first, int count, int stride, float* xyz) {
+    return guarded([&] {
+        if (!path) nsg::invalid("path is null");
+        if (count < 0 || stride < 1) nsg::invalid("need count >= 0 and stride >= 1");
+        nsg::DcdFile f(path);
+        const nsg::DcdInfo& I = f.info();
+        std::vector<unsigned char> buf(static_cast<size_t>(I.frame_bytes));
+        for (int i = 0; i < count; ++i) {
+            const long long fr = first + static_cast<long long>(i) * stride;
+            if (fr < 0 || fr >= I.nsets) nsg::invalid("frame outside the file");
+            f.read_frame(static_cast<int>(fr), buf.data());
+            f.check_frame(buf.data(), static_cast<int>(fr));
+            float* o = xyz + static_cast<size_t>(i) * 3 * I.natoms;
+            f.coordinates(buf.data(), o, o + I.natoms, o + 2 * I.natoms);
+        }
+    });
+}
+

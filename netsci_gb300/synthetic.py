@@ -109,3 +109,97 @@ def contact_graph(mean: np.ndarray, gc_pairs: np.ndarray, ab: np.ndarray,
             A[b, a] = w
     np.fill_diagonal(A, 0.0)
     return A
+
+
+# ---------------------------------------------------------------------------
+# Synthetic structure files: PDB topology + DCD trajectory
+# ---------------------------------------------------------------------------
+_RESIDUES = {  # residue name -> atom (name, element) list
+    "GLY": [("N", "N"), ("CA", "C"), ("C", "C"), ("O", "O")],
+    "ALA": [("N", "N"), ("CA", "C"), ("C", "C"), ("O", "O"), ("CB", "C")],
+    "SER": [("N", "N"), ("CA", "C"), ("C", "C"), ("O", "O"), ("CB", "C"), ("OG", "O")],
+    "CYS": [("N", "N"), ("CA", "C"), ("C", "C"), ("O", "O"), ("CB", "C"), ("SG", "S")],
+    "MET": [("N", "N"), ("H", "H"), ("CA", "C"), ("HA", "H"), ("C", "C"), ("O", "O"),
+            ("CB", "C"), ("CG", "C"), ("SD", "S"), ("CE", "C")],
+}
+
+
+def write_pdb(path, atoms) -> None:
+    """ATOM records in fixed PDB columns. atoms: dicts with name, resname,
+    chain, resid, x, y, z, occupancy, segment, element."""
+    with open(path, "w") as f:
+        f.write("CRYST1   50.000   50.000   50.000  90.00  90.00  90.00 P 1           1\n")
+        for i, a in enumerate(atoms):
+            f.write(f"ATOM  {(i + 1) % 100000:5d} {a['name']:<4s} {a['resname']:>3s} {a['chain']:1s}"
+                    f"{a['resid']:4d}    {a['x']:8.3f}{a['y']:8.3f}{a['z']:8.3f}"
+                    f"{a['occupancy']:6.2f}{0.0:6.2f}      {a['segment']:<4s}{a['element']:>2s}\n")
+        f.write("END\n")
+
+
+def write_dcd(path, frames: np.ndarray, charmm: bool = True, unit_cell: bool = True,
+              big_endian: bool = False, marker_bytes: int = 4, four_dims: bool = False) -> None:
+    """A DCD file of frames float32 [nsets, 3, natoms]."""
+    import struct
+    frames = np.asarray(frames, np.float32)
+    nsets, _, natoms = frames.shape
+    bo = ">" if big_endian else "<"
+    mk = bo + ("i" if marker_bytes == 4 else "q")
+
+    def rec(payload: bytes) -> bytes:
+        m = struct.pack(mk, len(payload))
+        return m + payload + m
+    words = [0] * 20
+    words[0], words[1], words[2], words[3] = nsets, 0, 1, nsets
+    if charmm:
+        words[10] = 1 if unit_cell else 0
+        words[11] = 1 if four_dims else 0
+        words[19] = 24
+    head = bytearray(b"CORD" + struct.pack(bo + "20i", *words))
+    if charmm:
+        head[4 + 36:4 + 40] = struct.pack(bo + "f", 1.0)
+    else:
+        head[4 + 36:4 + 44] = struct.pack(bo + "d", 1.0)
+    out = [rec(bytes(head)),
+           rec(struct.pack(bo + "i", 2) + b"synthetic trajectory".ljust(80) + b"netsci_gb300".ljust(80)),
+           rec(struct.pack(bo + "i", natoms))]
+    dt = np.dtype(np.float32).newbyteorder(bo)
+    for f in range(nsets):
+        if charmm and unit_cell:
+            out.append(rec(struct.pack(bo + "6d", 50.0, 90.0, 50.0, 90.0, 90.0, 50.0)))
+        for c in range(3):
+            out.append(rec(frames[f, c].astype(dt).tobytes()))
+        if charmm and four_dims:
+            out.append(rec(np.zeros(natoms, dt).tobytes()))
+    with open(path, "wb") as fh:
+        fh.write(b"".join(out))
+
+
+def protein_files(directory, n_residues: int, n_frames: int, seed: int, **dcd_kw):
+    """A synthetic protein (residues of 4-10 atoms of H, C, N, O, S, two
+    chains, one segment per chain) moving along a random walk with thermal
+    noise; writes <directory>/synthetic.pdb and .dcd and returns their
+    paths and the frames [n_frames, 3, natoms]."""
+    from pathlib import Path
+    rng = np.random.default_rng(seed)
+    names = list(_RESIDUES)
+    centres = self_avoiding_walk(n_residues, rng)
+    atoms, base = [], []
+    for r in range(n_residues):
+        rn = names[int(rng.integers(len(names)))]
+        chain = "A" if r < n_residues // 2 else "B"
+        for name, el in _RESIDUES[rn]:
+            p = centres[r] + rng.normal(0.0, 1.2, 3)
+            atoms.append(dict(name=name, resname=rn, chain=chain, resid=r % 9999 + 1, x=p[0],
+                              y=p[1], z=p[2], occupancy=1.0, segment="P" + chain, element=el))
+            base.append(p)
+    base = np.asarray(base, np.float32)
+    modes = rng.normal(0.0, 1.0, (3, len(atoms), 3)).astype(np.float32)
+    amp = rng.normal(0.0, 1.0, (n_frames, 3)).astype(np.float32)
+    xyz = base[None] + np.einsum("fk,kac->fac", amp, modes) \
+        + rng.normal(0.0, 0.3, (n_frames, len(atoms), 3)).astype(np.float32)
+    frames = np.ascontiguousarray(xyz.transpose(0, 2, 1)).astype(np.float32)
+    d = Path(directory)
+    pdb, dcd = d / "synthetic.pdb", d / "synthetic.dcd"
+    write_pdb(pdb, atoms)
+    write_dcd(dcd, frames, **dcd_kw)
+    return str(dcd), str(pdb), frames

@@ -217,3 +217,209 @@ def row_stats(a, n: int):
             q[:dv.size] = q[:dv.size] + dv * dv
         sigma[r] = np.sqrt(np.float32(_fold_1024(q) / nf), dtype=np.float32)
     return u, sigma
+
+
+# ---------------------------------------------------------------------------
+# netchem: PDB topology + DCD trajectory -> node centres of mass
+# ---------------------------------------------------------------------------
+_ATOMIC_WEIGHTS_G = {  # g/mol; netchem/include/chemical_properties.h:49-168 holds them / 1000
+    "H": "1.00794", "He": "4.002602", "Li": "6.941", "Be": "9.01218", "B": "10.811",
+    "C": "12.011", "N": "14.00674", "O": "15.9994", "F": "18.998403", "Ne": "20.1797",
+    "Na": "22.989768", "Mg": "24.305", "Al": "26.981539", "Si": "28.0855", "P": "30.973762",
+    "S": "32.066", "Cl": "35.4527", "Ar": "39.948", "K": "39.0983", "Ca": "40.078",
+    "Sc": "44.95591", "Ti": "47.88", "Cr": "51.9961", "Mn": "54.93805", "Fe": "55.847",
+    "Co": "58.9332", "Ni": "58.6934", "Cu": "63.546", "Zn": "65.39", "Ga": "69.723",
+    "Ge": "72.61", "As": "74.92159", "Se": "78.96", "Br": "79.904", "Kr": "83.8",
+    "Rb": "85.4678", "Sr": "87.62", "Y": "88.90585", "Zr": "91.224", "Nb": "92.90638",
+    "Mo": "95.94", "Tc": "97.9072", "Ru": "101.07", "Rh": "102.9055", "Pd": "106.42",
+    "Ag": "107.8682", "Cd": "112.411", "In": "114.818", "Sn": "118.71", "Sb": "121.76",
+    "Te": "127.6", "I": "126.90447", "Xe": "131.29", "Cs": "132.90543", "Ba": "137.327",
+    "La": "138.9055", "Ce": "140.115", "Pr": "140.90765", "Nd": "144.24", "Pm": "144.9127",
+    "Sm": "150.36", "Eu": "151.965", "Gd": "157.25", "Tb": "158.92534", "Dy": "162.5",
+    "Ho": "164.93032", "Er": "167.26", "Tm": "168.93421", "Yb": "173.04", "Lu": "174.967",
+    "Hf": "178.49", "Ta": "180.9479", "W": "183.84", "Re": "186.207", "Os": "190.23",
+    "Ir": "192.22", "Pt": "195.08", "Au": "196.96654", "Hg": "200.59", "Tl": "204.3833",
+    "Pb": "207.2", "Bi": "208.98037", "Po": "208.9824", "At": "209.9871", "Rn": "222.0176",
+    "Fr": "223.0197", "Ra": "226.0254", "Ac": "227.0278", "Th": "232.0381", "Pa": "231.03588",
+    "U": "238.0289", "Np": "237.048", "Pu": "244.0642", "Am": "243.0614", "Cm": "247.0703",
+    "Bk": "247.0703", "Cf": "251.0796", "Es": "252.083", "Fm": "257.0951", "Md": "258.1",
+    "No": "259.1009", "Lr": "262.11", "Rf": "261", "Db": "262", "Sg": "266", "Bh": "264",
+    "Hs": "269", "Mt": "268", "Ds": "269", "Rg": "272", "Cn": "277", "Nh": "0", "Fl": "289",
+    "Mc": "0", "Lv": "0", "Ts": "0", "Og": "0",
+}
+
+
+def atomic_weight_kg(symbol: str) -> float:
+    """kg/mol as the double the reference's table literal parses to."""
+    g = _ATOMIC_WEIGHTS_G.get(symbol)
+    return 0.0 if g is None else float(g + "e-3")
+
+
+def _hash_string(s: str) -> int:
+    """netchem/src/utils.cpp:94-110 with characters taken as signed."""
+    h = 37
+    for ch in s.encode():
+        c = ch - 256 if ch > 127 else ch
+        h = ((h * 54059) ^ ((c * 76963) & 0xFFFFFFFF)) & 0xFFFFFFFF
+    return h
+
+
+def pdb_atoms(path) -> list[dict]:
+    """ATOM records as netchem reads them (netchem/src/network.cpp:258-278,
+    netchem/src/atom.cpp:177-291)."""
+    out = []
+    with open(path, "r", newline="") as f:
+        for raw in f:
+            line = raw[:-1] if raw.endswith("\n") else raw
+            if "ATOM" not in line:
+                continue
+            idx = len(out)
+
+            def fld(p, n):
+                if p > len(line):
+                    raise ValueError(f"ATOM record {idx} too short")
+                return "".join(line[p:p + n].split())
+            el = fld(76, 2).lower()
+            el = el[:1].upper() + el[1:]
+            resid_s = fld(22, 4)
+            a = dict(index=idx, serial=idx + 1, name=fld(12, 3), residueName=fld(17, 3),
+                     chainId=fld(21, 1), residueId=int(resid_s), occupancy=np.float32(float(fld(54, 6))),
+                     segmentId=fld(72, 4), element=el)
+            a["temperatureFactor"] = a["occupancy"]
+            a["tag"] = f'{a["residueName"]}_{resid_s}_{a["chainId"]}_{a["segmentId"]}'
+            a["mass"] = np.float32(1000.0 * atomic_weight_kg(el))
+            a["hash"] = _hash_string(f'{idx}_{a["tag"]}')
+            out.append(a)
+    return out
+
+
+def dcd_read(path):
+    """(header dict, frames) with frames float32 [nsets, 3, natoms]: a DCD
+    reader written from the format (CHARMM / X-PLOR, 4- or 8-byte record
+    markers, either byte order; no fixed atoms)."""
+    b = Path(path).read_bytes()
+    import struct
+    for bo in ("<", ">"):
+        for mw in (4, 8):
+            fmt = bo + ("i" if mw == 4 else "q")
+            if len(b) >= mw + 4 and struct.unpack(fmt, b[:mw])[0] == 84 and b[mw:mw + 4] == b"CORD":
+                break
+        else:
+            continue
+        break
+    else:
+        raise ValueError("not a DCD file")
+    mk = bo + ("i" if mw == 4 else "q")
+
+    def marker(p):
+        return struct.unpack(mk, b[p:p + mw])[0]
+    words = struct.unpack(bo + "20i", b[mw + 4:mw + 84])
+    charmm = words[19] != 0
+    cell = charmm and words[10] != 0
+    four = charmm and words[11] == 1
+    if words[8] != 0:
+        raise ValueError("fixed atoms")
+    p = mw + 84
+    assert marker(p) == 84
+    p += mw
+    tlen = marker(p)
+    p += mw + tlen
+    assert marker(p) == tlen
+    p += mw
+    assert marker(p) == 4
+    natoms = struct.unpack(bo + "i", b[p + mw:p + mw + 4])[0]
+    p += mw + 4
+    assert marker(p) == 4
+    p += mw
+    rec = 2 * mw + 4 * natoms
+    fb = (2 * mw + 48 if cell else 0) + (4 if four else 3) * rec
+    nsets = (len(b) - p) // fb
+    frames = np.empty((nsets, 3, natoms), np.float32)
+    dt = np.dtype(np.float32).newbyteorder(bo)
+    for f in range(nsets):
+        q = p + f * fb + (2 * mw + 48 if cell else 0)
+        for c in range(3):
+            assert marker(q) == 4 * natoms
+            frames[f, c] = np.frombuffer(b, dt, natoms, q + mw)
+            q += rec
+    return dict(natoms=natoms, nsets=nsets, charmm=charmm, unit_cell=cell, header_nsets=words[0]), frames
+
+
+def node_coordinates(trajectory, topology, first: int, last: int, stride: int = 1):
+    """(X, nodes): X float32 [N, 3m] of node mass-weighted centres, nodes a
+    list of (tag, atom indices, total mass): netchem/src/network.cpp:29-255,
+    float32 arithmetic in the same order (per node, atoms in index order,
+    acc = acc + x * mass, then / total mass)."""
+    atoms = pdb_atoms(topology)
+    _, frames = dcd_read(trajectory)
+    if last == -1:
+        last = frames.shape[0] - 1
+    sel = np.arange(first, last + 1, stride)
+    fr = frames[sel]
+    tags, members = {}, []
+    for a in atoms:
+        if a["tag"] not in tags:
+            tags[a["tag"]] = len(members)
+            members.append([])
+        members[tags[a["tag"]]].append(a["index"])
+    N, m = len(members), len(sel)
+    X = np.zeros((N, 3, m), np.float32)
+    nodes = []
+    for n, mem in enumerate(members):
+        tm = np.float32(0)
+        acc = np.zeros((3, m), np.float32)
+        for ai in mem:
+            w = atoms[ai]["mass"]
+            tm = np.float32(tm + w)
+            acc = acc + fr[:, :, ai].T * w
+        X[n] = acc / tm
+        nodes.append((atoms[mem[0]]["tag"], mem, tm))
+    return X.reshape(N, 3 * m), nodes
+
+
+def ref_netchem():
+    """The reference's DCD plugin and Atom class compiled into
+    ``_ref/libnetchem_ref.so`` (None when absent)."""
+    p = HERE / "_ref" / "libnetchem_ref.so"
+    if not p.exists():
+        return None
+    L = ctypes.CDLL(str(p))
+    L.ref_dcd_frames.restype = ctypes.c_int
+    L.ref_dcd_frames.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
+                                 ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
+    L.ref_pdb_atoms.restype = ctypes.c_int
+    L.ref_pdb_atoms.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+    return L
+
+
+def ref_dcd_frames(path):
+    """float32 [nsets, 3, natoms] through the reference's DCD plugin."""
+    L = ref_netchem()
+    na, ns = ctypes.c_int(), ctypes.c_int()
+    assert L.ref_dcd_frames(str(path).encode(), ctypes.byref(na), ctypes.byref(ns), None) == 0
+    out = np.zeros((ns.value, 3, na.value), np.float32)
+    rc = L.ref_dcd_frames(str(path).encode(), ctypes.byref(na), ctypes.byref(ns),
+                          out.ctypes.data_as(ctypes.c_void_p))
+    assert rc == 0, rc
+    return out
+
+
+def ref_pdb_atoms(path, cap: int = 200000):
+    """(mass, residue id, hash, tags, elements, names) from the reference's Atom."""
+    L = ref_netchem()
+    mass = np.zeros(cap, np.float32)
+    resid = np.zeros(cap, np.int32)
+    h = np.zeros(cap, np.uint32)
+    tags = ctypes.create_string_buffer(40 * cap)
+    els = ctypes.create_string_buffer(4 * cap)
+    names = ctypes.create_string_buffer(8 * cap)
+    n = L.ref_pdb_atoms(str(path).encode(), cap, mass.ctypes.data_as(ctypes.c_void_p),
+                        resid.ctypes.data_as(ctypes.c_void_p), h.ctypes.data_as(ctypes.c_void_p),
+                        tags, els, names)
+    n = min(n, cap)
+
+    def strs(buf, w):
+        raw = buf.raw
+        return [raw[w * i:w * (i + 1)].split(b"\0")[0].decode() for i in range(n)]
+    return mass[:n], resid[:n], h[:n], strs(tags, 40), strs(els, 4), strs(names, 8)
