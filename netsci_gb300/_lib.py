@@ -131,6 +131,8 @@ _SIGNATURES = {
     "nsg_ksg_set_shape": (c_int, [c_int, c_int, c_int, c_int]),
     "nsg_ksg_set_staging": (c_int, [c_int]),
     "nsg_ksg_plan_staging": (c_int, [c_void_p, P_int]),
+    "nsg_ksg_set_search": (c_int, [c_int]),
+    "nsg_ksg_plan_search": (c_int, [c_void_p, P_int]),
     "nsg_server_create": (c_int, [c_size_t, c_double, c_int, PP_void]),
     "nsg_server_destroy": (c_int, [c_void_p]),
     "nsg_server_register_trajectory": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, P_int]),

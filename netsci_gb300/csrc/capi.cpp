@@ -494,6 +494,13 @@ int nsg_ksg_plan_staging(const nsg_ksg_plan* plan, int* staging) {
     });
 }
 
+int nsg_ksg_plan_search(const nsg_ksg_plan* plan, int* mode) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        *mode = plan->plan->search();
+    });
+}
+
 int nsg_ksg_plan_check(nsg_ksg_plan* plan) {
     return guarded([&] {
         if (!plan || !plan->plan) nsg::invalid("plan is null");
@@ -538,6 +545,13 @@ int nsg_ksg_set_staging(int staging) {
     return guarded([&] {
         if (staging < -1 || staging > 1) nsg::invalid("staging must be -1, 0 or 1");
         nsg::ksg_force_staging(staging);
+    });
+}
+
+int nsg_ksg_set_search(int mode) {
+    return guarded([&] {
+        if (mode < -1 || mode > 1) nsg::invalid("search must be -1, 0 or 1");
+        nsg::ksg_force_search(mode);
     });
 }
 

@@ -11,6 +11,7 @@
 #include <string>
 
 #include "errors.h"
+#include "ksg_grid.h"
 #include "ksg_registry.cuh"
 
 namespace nsg {
@@ -73,6 +74,12 @@ std::mutex g_shape_mu;
 KsgShape g_forced{0, 0, 0};
 int g_forced_variant = -1;
 int g_forced_staging = -1;
+int g_forced_search = -1;
+// Below this many samples per pair the exhaustive kernel is used: grids of
+// a few cells per axis prune little.
+constexpr int kGridMinSamples = 2048;
+// per batch: work-queue heads (two for the grid search), tie count, tie-kernel counter
+constexpr int kCounters = 4;
 }  // namespace
 
 std::shared_ptr<const DeviceBuffer> device_psi(int n) {
@@ -98,6 +105,11 @@ void ksg_force_shape(int threads, int r, int frames, int variant) {
     std::lock_guard<std::mutex> lk(g_shape_mu);
     g_forced = {threads, r, frames};
     g_forced_variant = variant;
+}
+
+void ksg_force_search(int mode) {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    g_forced_search = mode;
 }
 
 void ksg_force_staging(int staging) {
@@ -175,6 +187,24 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
     if (kmax_ == 0) fail(NSG_ERR_UNSUPPORTED, "k > 62 is not supported by the GPU path");
     const bool per_sample = out.nx || out.ny || out.eps_x || out.eps_y || out.kdist;
 
+    // ---- search: cell grids when every pair allows them -------------------
+    int search = opt.search;
+    if (search < 0) {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        search = g_forced_search;
+    }
+    bool grid_ok = npairs > 0;
+    int minm = maxm;
+    for (const auto& q : pairs) {
+        if (q.fmap) grid_ok = false;
+        minm = std::min(minm, q.m);
+    }
+    if (search == 1 && !grid_ok) {
+        fail(NSG_ERR_UNSUPPORTED, "cell-grid search needs pairs without frame maps");
+    }
+    if (search < 0) search = (grid_ok && minm >= kGridMinSamples) ? 1 : 0;
+    search_ = search == 1 ? 1 : 0;
+
     // ---- tile shape -----------------------------------------------------
     // explicit per-plan shape, then the process-wide override, then the
     // autotuner, then the preference order below
@@ -195,7 +225,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
     }
     const bool bulk_ok = ksg_bulk_copy_ok(pairs);
     int tuned_staging = -1;
-    if (!shape_.threads && opt.autotune && npairs > 0) {
+    if (!shape_.threads && opt.autotune && npairs > 0 && !search_) {
         const KsgTuned t = ksg_autotune(pairs, k, d);
         shape_ = t.shape;
         variant_ = t.variant;
@@ -267,8 +297,12 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
     std::vector<long long> prefix(npairs + 1, 0);
     for (int p = 0; p < npairs; ++p) prefix[p + 1] = prefix[p] + pairs[p].m;
 
-    size_t budget = opt.scratch_budget_bytes ? opt.scratch_budget_bytes : (size_t(1) << 31);
+    size_t budget = opt.scratch_budget_bytes ? opt.scratch_budget_bytes
+                                             : (size_t(1) << (search_ ? 32 : 31));
     long long budget_floats = static_cast<long long>(budget / sizeof(float));
+    // cell grids: eps and counts per sample plus the batch's pair grids
+    // (2d coordinates and an index per sample) on top of the psi sums
+    if (search_) budget_floats = static_cast<long long>(budget / (sizeof(float) * (5 + 2 * d + 1)));
     if (per_sample) budget_floats = std::max<long long>(budget_floats, total_samples);
 
     std::vector<KsgPairDesc> descs(npairs);
@@ -315,7 +349,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
                             cudaMemcpyHostToDevice));
         scratch_.reset(static_cast<size_t>(scratch_need) * sizeof(float));
         // per batch: work-queue head, tie count, tie-kernel work counter
-        counters_.reset(3 * batches_.size() * sizeof(int));
+        counters_.reset(kCounters * batches_.size() * sizeof(int));
         // Samples with an ambiguous tie are rare (about 1e-4 on trajectory
         // data; ties among copies of one frame are not listed); the list
         // holds a quarter of the largest batch's samples.
@@ -334,6 +368,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         fault_.reset(sizeof(int));
         NSG_CUDA(cudaMemset(fault_.get(), 0, sizeof(int)));
         psi_ = device_psi(maxm);
+        if (search_) setup_grid(descs);
     }
     if (timing_) {
         events_.resize(2 * batches_.size());
@@ -349,10 +384,14 @@ KsgPlan::~KsgPlan() {
 
 void KsgPlan::enqueue(cudaStream_t s) {
     if (batches_.empty()) return;
-    NSG_CUDA(cudaMemsetAsync(counters_.get(), 0, 3 * batches_.size() * sizeof(int), s));
+    NSG_CUDA(cudaMemsetAsync(counters_.get(), 0, kCounters * batches_.size() * sizeof(int), s));
+    if (search_) {
+        enqueue_grid(s);
+        return;
+    }
     for (size_t bi = 0; bi < batches_.size(); ++bi) {
         const Batch& b = batches_[bi];
-        int* ctr = counters_.as<int>() + 3 * bi;
+        int* ctr = counters_.as<int>() + kCounters * bi;
         KsgCountArgs a{};
         a.pairs = pairs_dev_.as<KsgPairDesc>();
         a.items = items_dev_.as<KsgItem>() + b.item0;
@@ -395,6 +434,196 @@ void KsgPlan::enqueue(cudaStream_t s) {
         ksg_launch_ties(t, d_, s);
         KsgFinalArgs f{};
         f.pairs = pairs_dev_.as<KsgPairDesc>() + b.pair0;
+        f.npairs = b.npairs;
+        f.k = k_;
+        f.d = d_;
+        f.psi = psi_->as<float>();
+        f.psum = scratch_.as<float>();
+        f.mi = out_.mi;
+        f.gc = out_.gc;
+        f.w = out_.w;
+        ksg_launch_final(f, s);
+    }
+}
+
+// ---- cell-grid search ---------------------------------------------------------
+struct KsgPlan::GridState {
+    DeviceBuffer nodes, node_arena;       // GridNode[nnodes] and their buffers
+    DeviceBuffer gps, pair_arena;         // GridPair per plan pair; pair grids of one batch
+    DeviceBuffer wprefix;                 // per batch: npairs+1 prefix of ceil(m/32)
+    std::vector<long long> wprefix_off;   // offset of each batch's prefix
+    DeviceBuffer eps_a, eps_b, cnt_a, cnt_b;
+    int nnodes = 0;
+    int search_grid = 0, count_grid = 0;
+};
+
+namespace {
+size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+}  // namespace
+
+void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
+    auto g = std::make_shared<GridState>();
+    // nodes: one per distinct (row, m, ld)
+    struct Key {
+        const float* x;
+        int m, ld;
+        bool operator<(const Key& o) const {
+            if (x != o.x) return x < o.x;
+            if (m != o.m) return m < o.m;
+            return ld < o.ld;
+        }
+    };
+    std::map<Key, int> ids;
+    std::vector<GridNode> nodes;
+    std::vector<size_t> node_off;
+    size_t arena = 0;
+    auto node_id = [&](const float* x, int m, int ld) {
+        auto it = ids.find({x, m, ld});
+        if (it != ids.end()) return it->second;
+        const int id = static_cast<int>(nodes.size());
+        ids.emplace(Key{x, m, ld}, id);
+        GridNode n{};
+        n.x = x;
+        n.ld = ld;
+        n.m = m;
+        n.G = grid_cells_per_axis(m);
+        nodes.push_back(n);
+        node_off.push_back(arena);
+        const size_t cells = static_cast<size_t>(n.G) * n.G + 1;
+        arena += align16(2 * kGridMaxG * sizeof(float)) + align16(cells * sizeof(int)) +
+                 align16(static_cast<size_t>(m) * sizeof(unsigned short)) +
+                 align16(static_cast<size_t>(m) * sizeof(int)) +
+                 align16(static_cast<size_t>(d_) * m * sizeof(float));
+        return id;
+    };
+    std::vector<GridPair> gps(descs.size());
+    for (size_t p = 0; p < descs.size(); ++p) {
+        gps[p].a = node_id(descs[p].xa, descs[p].m, descs[p].ld);
+        gps[p].b = node_id(descs[p].xb, descs[p].m, descs[p].ld);
+    }
+    g->nnodes = static_cast<int>(nodes.size());
+    g->node_arena.reset(std::max<size_t>(arena, 16));
+    unsigned char* base = g->node_arena.as<unsigned char>();
+    for (size_t i = 0; i < nodes.size(); ++i) {
+        GridNode& n = nodes[i];
+        unsigned char* q = base + node_off[i];
+        const size_t cells = static_cast<size_t>(n.G) * n.G + 1;
+        n.e1 = reinterpret_cast<float*>(q);
+        n.e2 = n.e1 + kGridMaxG;
+        q += align16(2 * kGridMaxG * sizeof(float));
+        n.start = reinterpret_cast<int*>(q);
+        q += align16(cells * sizeof(int));
+        n.cell = reinterpret_cast<unsigned short*>(q);
+        q += align16(static_cast<size_t>(n.m) * sizeof(unsigned short));
+        n.perm = reinterpret_cast<int*>(q);
+        q += align16(static_cast<size_t>(n.m) * sizeof(int));
+        n.sx = reinterpret_cast<float*>(q);
+    }
+    g->nodes.reset(nodes.size() * sizeof(GridNode));
+    NSG_CUDA(cudaMemcpy(g->nodes.get(), nodes.data(), nodes.size() * sizeof(GridNode),
+                        cudaMemcpyHostToDevice));
+
+    // pair grids: every batch reuses one arena sized for the largest batch
+    size_t pair_arena = 0;
+    std::vector<int> wpre;
+    for (const Batch& b : batches_) {
+        size_t off = 0;
+        g->wprefix_off.push_back(static_cast<long long>(wpre.size()));
+        int acc = 0;
+        for (int p = b.pair0; p < b.pair0 + b.npairs; ++p) {
+            wpre.push_back(acc);
+            acc += (descs[p].m + 31) / 32;
+            const int G = nodes[gps[p].a].G;
+            const size_t cells = static_cast<size_t>(G) * G + 1;
+            gps[p].start = reinterpret_cast<int*>(off);
+            off += align16(cells * sizeof(int));
+            gps[p].perm = reinterpret_cast<int*>(off);
+            off += align16(static_cast<size_t>(descs[p].m) * sizeof(int));
+            gps[p].sx = reinterpret_cast<float*>(off);
+            off += align16(static_cast<size_t>(2 * d_) * descs[p].m * sizeof(float));
+        }
+        wpre.push_back(acc);
+        pair_arena = std::max(pair_arena, off);
+    }
+    g->pair_arena.reset(std::max<size_t>(pair_arena, 16));
+    const uintptr_t pbase = reinterpret_cast<uintptr_t>(g->pair_arena.get());
+    for (auto& gp : gps) {
+        gp.start = reinterpret_cast<int*>(pbase + reinterpret_cast<uintptr_t>(gp.start));
+        gp.perm = reinterpret_cast<int*>(pbase + reinterpret_cast<uintptr_t>(gp.perm));
+        gp.sx = reinterpret_cast<float*>(pbase + reinterpret_cast<uintptr_t>(gp.sx));
+    }
+    g->gps.reset(gps.size() * sizeof(GridPair));
+    NSG_CUDA(cudaMemcpy(g->gps.get(), gps.data(), gps.size() * sizeof(GridPair), cudaMemcpyHostToDevice));
+    g->wprefix.reset(wpre.size() * sizeof(int));
+    NSG_CUDA(cudaMemcpy(g->wprefix.get(), wpre.data(), wpre.size() * sizeof(int), cudaMemcpyHostToDevice));
+    const size_t ns = scratch_.bytes() / sizeof(float);
+    g->eps_a.reset(ns * sizeof(float));
+    g->eps_b.reset(ns * sizeof(float));
+    g->cnt_a.reset(ns * sizeof(int));
+    g->cnt_b.reset(ns * sizeof(int));
+    g->search_grid = sm_count() * grid_search_ctas_per_sm(d_, kmax_);
+    g->count_grid = sm_count() * grid_count_ctas_per_sm(d_);
+    grid_ = std::move(g);
+    shape_ = {32 * kGridWarps, 1, kGridChunk};
+    variant_ = 1;
+}
+
+void KsgPlan::enqueue_grid(cudaStream_t s) {
+    GridState& g = *grid_;
+    grid_launch_nodes(g.nodes.as<GridNode>(), g.nnodes, d_, s);
+    for (size_t bi = 0; bi < batches_.size(); ++bi) {
+        const Batch& b = batches_[bi];
+        int* ctr = counters_.as<int>() + kCounters * bi;
+        KsgPairDesc* bp = pairs_dev_.as<KsgPairDesc>() + b.pair0;
+        GridPair* bg = g.gps.as<GridPair>() + b.pair0;
+        grid_launch_pairs(bp, bg, g.nodes.as<GridNode>(), b.npairs, d_, s);
+        GridArgs a{};
+        a.pairs = bp;
+        a.gp = bg;
+        a.nodes = g.nodes.as<GridNode>();
+        a.wprefix = g.wprefix.as<int>() + g.wprefix_off[bi];
+        a.npairs = b.npairs;
+        a.pair_base = b.pair0;
+        a.k = k_;
+        a.counter = ctr;
+        a.fault = fault_.as<int>();
+        a.ties = ties_.as<KsgTie>();
+        a.tie_count = ctr + 2;
+        a.tie_cap = tie_cap_;
+        a.eps_a = g.eps_a.as<float>();
+        a.eps_b = g.eps_b.as<float>();
+        a.cnt_a = g.cnt_a.as<int>();
+        a.cnt_b = g.cnt_b.as<int>();
+        a.eps_x = out_.eps_x;
+        a.eps_y = out_.eps_y;
+        a.kdist = out_.kdist;
+        if (timing_) record_event(events_[2 * bi], s);
+        grid_launch_search(a, d_, kmax_, g.search_grid, s);
+        a.counter = ctr + 1;
+        grid_launch_counts(a, d_, g.count_grid, s);
+        if (timing_) record_event(events_[2 * bi + 1], s);
+        grid_launch_combine(bp, b.npairs, g.cnt_a.as<int>(), g.cnt_b.as<int>(), psi_->as<float>(),
+                            scratch_.as<float>(), out_.nx, out_.ny, s);
+        KsgTieArgs t{};
+        t.pairs = pairs_dev_.as<KsgPairDesc>();
+        t.ties = ties_.as<KsgTie>();
+        t.tie_count = ctr + 2;
+        t.tie_cap = tie_cap_;
+        t.tie_next = ctr + 3;
+        t.k = k_;
+        t.fault = fault_.as<int>();
+        t.psi = psi_->as<float>();
+        t.psum = scratch_.as<float>();
+        t.nx = out_.nx;
+        t.ny = out_.ny;
+        t.eps_x = out_.eps_x;
+        t.eps_y = out_.eps_y;
+        t.dz = tie_dz_.as<float>();
+        t.idx = tie_idx_.as<int>();
+        t.stride = tie_stride_;
+        ksg_launch_ties(t, d_, s);
+        KsgFinalArgs f{};
+        f.pairs = bp;
         f.npairs = b.npairs;
         f.k = k_;
         f.d = d_;

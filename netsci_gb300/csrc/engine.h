@@ -55,6 +55,7 @@ struct KsgPlanOptions {
     KsgShape shape{0, 0, 0};             // explicit shape (threads == 0: choose)
     int variant = -1;
     int staging = -1;                    // -1 auto, 0 plain loads, 1 bulk copies (TMA)
+    int search = -1;                     // -1 auto, 0 exhaustive, 1 cell grids
     size_t scratch_budget_bytes = 0;     // 0: library default
 };
 
@@ -66,8 +67,13 @@ public:
     void run(cudaStream_t s);
     // Captures and instantiates the run's CUDA graph now (graph plans only).
     void prepare();
-    // Kernel launches per run: count, tie resolution and finalize per batch.
-    int launches() const { return 3 * static_cast<int>(batches_.size()); }
+    // Kernel launches per run: count, tie resolution and finalize per batch
+    // (exhaustive search); node grids once, then pair grids, search, counts,
+    // combine, ties and finalize per batch (cell-grid search).
+    int launches() const {
+        const int nb = static_cast<int>(batches_.size());
+        return search_ == 1 ? (nb ? 1 + 6 * nb : 0) : 3 * nb;
+    }
     // Device time of the count kernels of the last run (ms); needs timing.
     float count_ms() const;
     long long pairs() const { return npairs_; }
@@ -76,6 +82,7 @@ public:
     const KsgShape& shape() const { return shape_; }
     int variant() const { return variant_; }
     int staging() const;  // 1: bulk-copy staged kernel, 0: plain loads
+    int search() const { return search_; }  // 1: cell grids, 0: exhaustive
 
 private:
     struct Batch {
@@ -84,6 +91,8 @@ private:
         int grid = 0;
     };
     void enqueue(cudaStream_t s);
+    void enqueue_grid(cudaStream_t s);
+    void setup_grid(const std::vector<KsgPairDesc>& descs);
 
     int d_, k_, kmax_;
     long long npairs_ = 0;
@@ -98,6 +107,9 @@ private:
     DeviceBuffer ties_, tie_dz_, tie_idx_;
     int tie_cap_ = 0;
     long long tie_stride_ = 0;
+    int search_ = 0;
+    struct GridState;
+    std::shared_ptr<GridState> grid_;
     std::shared_ptr<const DeviceBuffer> psi_;
     bool graph_ = false;
     cudaGraphExec_t exec_ = nullptr;
@@ -124,6 +136,9 @@ KsgTuned ksg_autotune(const std::vector<nsg_ksg_pair>& pairs, int k, int d);
 void ksg_force_shape(int threads, int r, int frames, int variant);
 // Staging override set by nsg_ksg_set_staging (-1 automatic).
 void ksg_force_staging(int staging);
+// Search override set by nsg_ksg_set_search (-1 automatic, 0 exhaustive,
+// 1 cell grids).
+void ksg_force_search(int mode);
 // True when every pair allows bulk-copy staging (16-byte aligned rows,
 // plane stride a multiple of 4, no frame map).
 bool ksg_bulk_copy_ok(const std::vector<nsg_ksg_pair>& pairs);

@@ -1,0 +1,312 @@
+// Cell-grid KSG: grid construction kernels, the instantiations of the grid
+// pass-1 / count kernels and their launchers (ksg_grid.cuh has the search).
+#include <cuda_runtime.h>
+
+#include "errors.h"
+#include "ksg_grid.cuh"
+#include "ksg_grid.h"
+
+namespace nsg {
+namespace {
+
+constexpr int kPrepThreads = 1024;
+constexpr int kSample = 2048;       // frames sampled per coordinate for the quantiles
+
+// In-place ascending bitonic sort of n = kSample floats in shared memory.
+__device__ void bitonic_sort(float* v) {
+    for (int size = 2; size <= kSample; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < kSample / 2; t += blockDim.x) {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const float a = v[lo], b = v[hi];
+                if ((a > b) == asc) {
+                    v[lo] = b;
+                    v[hi] = a;
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Number of edges <= x among e[0..n) (sorted ascending): the bin of x.
+__device__ __forceinline__ int bin_of(const float* e, int n, float x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (e[mid] <= x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Exclusive scan of cnt[0..n) (n <= 1024) into out[0..n], out[n] = total.
+__device__ void block_scan(const int* cnt, int* out, int n) {
+    __shared__ int s_warp[32];
+    const int t = threadIdx.x;
+    const int v = t < n ? cnt[t] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((t & 31) >= o) x += y;
+    }
+    if ((t & 31) == 31) s_warp[t >> 5] = x;
+    __syncthreads();
+    if (t < 32) {
+        int w = t < (blockDim.x >> 5) ? s_warp[t] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (t >= o) w += y;
+        }
+        s_warp[t] = w;
+    }
+    __syncthreads();
+    const int incl = x + ((t >> 5) ? s_warp[(t >> 5) - 1] : 0);
+    if (t < n) out[t] = incl - v;
+    if (t == n - 1) out[n] = incl;
+    __syncthreads();
+}
+
+// One CTA per node: axes, quantile edges, cells, counting sort by cell.
+template <int D>
+__global__ void __launch_bounds__(kPrepThreads) grid_node_kernel(GridNode* nodes) {
+    __shared__ float s_val[D][kSample];
+    __shared__ float s_e1[kGridMaxG], s_e2[kGridMaxG];
+    __shared__ int s_cnt[kGridMaxG * kGridMaxG];
+    __shared__ int s_start[kGridMaxG * kGridMaxG + 1];
+    __shared__ int s_axis[2];
+    GridNode nd = nodes[blockIdx.x];
+    const int m = nd.m, G = nd.G, t = threadIdx.x;
+    const int S = kSample;
+    for (int s = t; s < S; s += blockDim.x) {
+        const int j = static_cast<int>((static_cast<long long>(s) * m) / S);
+#pragma unroll
+        for (int c = 0; c < D; ++c) s_val[c][s] = __ldg(nd.x + static_cast<long long>(c) * nd.ld + j);
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) bitonic_sort(s_val[c]);
+    if (t == 0) {
+        // widest and second-widest coordinates by their 10-90% spread
+        float w[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) w[c] = s_val[c][(S * 9) / 10] - s_val[c][S / 10];
+        int c1 = 0;
+        for (int c = 1; c < D; ++c)
+            if (w[c] > w[c1]) c1 = c;
+        int c2 = -1;
+        for (int c = 0; c < D; ++c)
+            if (c != c1 && (c2 < 0 || w[c] > w[c2])) c2 = c;
+        s_axis[0] = c1;
+        s_axis[1] = c2;
+    }
+    __syncthreads();
+    const int c1 = s_axis[0], c2 = s_axis[1];
+    if (t < kGridMaxG) {
+        const float inf = __int_as_float(0x7f800000);
+        s_e1[t] = t < G - 1 ? s_val[c1][((t + 1) * S) / G] : inf;
+        s_e2[t] = (c2 >= 0 && t < G - 1) ? s_val[c2][((t + 1) * S) / G] : inf;
+        nd.e1[t] = s_e1[t];
+        nd.e2[t] = s_e2[t];
+    }
+    if (t == 0) {
+        nodes[blockIdx.x].c1 = c1;
+        nodes[blockIdx.x].c2 = c2;
+    }
+    for (int c = t; c < G * G; c += blockDim.x) s_cnt[c] = 0;
+    __syncthreads();
+    const float* x1 = nd.x + static_cast<long long>(c1) * nd.ld;
+    const float* x2 = c2 >= 0 ? nd.x + static_cast<long long>(c2) * nd.ld : nullptr;
+    for (int j = t; j < m; j += blockDim.x) {
+        const int b1 = bin_of(s_e1, G - 1, __ldg(x1 + j));
+        const int b2 = x2 ? bin_of(s_e2, G - 1, __ldg(x2 + j)) : 0;
+        const int cell = b1 * G + b2;
+        nd.cell[j] = static_cast<unsigned short>(cell);
+        atomicAdd(&s_cnt[cell], 1);
+    }
+    __syncthreads();
+    block_scan(s_cnt, s_start, G * G);
+    for (int c = t; c <= G * G; c += blockDim.x) nd.start[c] = s_start[c];
+    for (int c = t; c < G * G; c += blockDim.x) s_cnt[c] = 0;
+    __syncthreads();
+    for (int j = t; j < m; j += blockDim.x) {
+        const int cell = nd.cell[j];
+        const int pos = s_start[cell] + atomicAdd(&s_cnt[cell], 1);
+        nd.perm[pos] = j;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            nd.sx[static_cast<long long>(c) * m + pos] = __ldg(nd.x + static_cast<long long>(c) * nd.ld + j);
+        }
+    }
+}
+
+// One CTA per pair of the batch: cells over (bin of a on its c1, bin of b on
+// its c1), counting sort, both nodes' coordinates copied in that order.
+template <int D>
+__global__ void __launch_bounds__(kPrepThreads) grid_pair_kernel(const KsgPairDesc* pairs,
+                                                                GridPair* gps,
+                                                                const GridNode* nodes) {
+    __shared__ int s_cnt[kGridMaxG * kGridMaxG];
+    __shared__ int s_start[kGridMaxG * kGridMaxG + 1];
+    const KsgPairDesc P = pairs[blockIdx.x];
+    const GridPair gp = gps[blockIdx.x];
+    const GridNode na = nodes[gp.a], nb = nodes[gp.b];
+    const int m = P.m, G = na.G, t = threadIdx.x;
+    for (int c = t; c < G * G; c += blockDim.x) s_cnt[c] = 0;
+    __syncthreads();
+    for (int j = t; j < m; j += blockDim.x) {
+        const int cell = (na.cell[j] / G) * G + nb.cell[j] / G;
+        atomicAdd(&s_cnt[cell], 1);
+    }
+    __syncthreads();
+    block_scan(s_cnt, s_start, G * G);
+    for (int c = t; c <= G * G; c += blockDim.x) gp.start[c] = s_start[c];
+    for (int c = t; c < G * G; c += blockDim.x) s_cnt[c] = 0;
+    __syncthreads();
+    for (int j = t; j < m; j += blockDim.x) {
+        const int cell = (na.cell[j] / G) * G + nb.cell[j] / G;
+        const int pos = s_start[cell] + atomicAdd(&s_cnt[cell], 1);
+        gp.perm[pos] = j;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            gp.sx[static_cast<long long>(c) * m + pos] = __ldg(P.xa + static_cast<long long>(c) * P.ld + j);
+            gp.sx[static_cast<long long>(D + c) * m + pos] =
+                __ldg(P.xb + static_cast<long long>(c) * P.ld + j);
+        }
+    }
+}
+
+// psi[n_x] + psi[n_y] per sample from the raw counts (self included), as
+// write_outputs does in the exhaustive kernel.
+__global__ void grid_combine_kernel(const KsgPairDesc* pairs, const int* cnt_a, const int* cnt_b,
+                                    const float* psi, float* psum, int* nx_out, int* ny_out) {
+    const KsgPairDesc P = pairs[blockIdx.x];
+    for (int i = threadIdx.x; i < P.m; i += blockDim.x) {
+        const long long o = P.scratch + i;
+        const int nx = min(max(cnt_a[o] - 1, 0), P.m);
+        const int ny = min(max(cnt_b[o] - 1, 0), P.m);
+        psum[o] = __fadd_rn(__ldg(psi + nx), __ldg(psi + ny));
+        if (nx_out) nx_out[o] = nx;
+        if (ny_out) ny_out[o] = ny;
+    }
+}
+
+template <int D>
+void launch_pass1(const GridArgs& a, int kmax, int grid, cudaStream_t st) {
+    const dim3 b(32 * kGridWarps);
+    switch (kmax) {
+        case 6: ksg_grid_pass1_kernel<D, 6><<<grid, b, 0, st>>>(a); break;
+        case 8: ksg_grid_pass1_kernel<D, 8><<<grid, b, 0, st>>>(a); break;
+        case 16: ksg_grid_pass1_kernel<D, 16><<<grid, b, 0, st>>>(a); break;
+        case 32: ksg_grid_pass1_kernel<D, 32><<<grid, b, 0, st>>>(a); break;
+        case 64: ksg_grid_pass1_kernel<D, 64><<<grid, b, 0, st>>>(a); break;
+        default: fail(NSG_ERR_UNSUPPORTED, "no grid kernel for this k");
+    }
+}
+
+}  // namespace
+
+int grid_cells_per_axis(int m) {
+    int g = 1;
+    while ((g + 1) * (g + 1) * 10 <= m && g < kGridMaxG) ++g;
+    return g;
+}
+
+void grid_launch_nodes(GridNode* nodes, int nnodes, int d, cudaStream_t st) {
+    if (nnodes <= 0) return;
+    switch (d) {
+        case 1: grid_node_kernel<1><<<nnodes, kPrepThreads, 0, st>>>(nodes); break;
+        case 2: grid_node_kernel<2><<<nnodes, kPrepThreads, 0, st>>>(nodes); break;
+        case 3: grid_node_kernel<3><<<nnodes, kPrepThreads, 0, st>>>(nodes); break;
+        default: invalid("d must be 1, 2 or 3");
+    }
+    NSG_CUDA(cudaGetLastError());
+}
+
+void grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
+                       int d, cudaStream_t st) {
+    if (npairs <= 0) return;
+    switch (d) {
+        case 1: grid_pair_kernel<1><<<npairs, kPrepThreads, 0, st>>>(pairs, gps, nodes); break;
+        case 2: grid_pair_kernel<2><<<npairs, kPrepThreads, 0, st>>>(pairs, gps, nodes); break;
+        case 3: grid_pair_kernel<3><<<npairs, kPrepThreads, 0, st>>>(pairs, gps, nodes); break;
+        default: invalid("d must be 1, 2 or 3");
+    }
+    NSG_CUDA(cudaGetLastError());
+}
+
+void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st) {
+    switch (d) {
+        case 1: launch_pass1<1>(a, kmax, grid, st); break;
+        case 2: launch_pass1<2>(a, kmax, grid, st); break;
+        case 3: launch_pass1<3>(a, kmax, grid, st); break;
+        default: invalid("d must be 1, 2 or 3");
+    }
+    NSG_CUDA(cudaGetLastError());
+}
+
+void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st) {
+    const dim3 b(32 * kGridWarps);
+    switch (d) {
+        case 1: ksg_grid_count_kernel<1><<<grid, b, 0, st>>>(a); break;
+        case 2: ksg_grid_count_kernel<2><<<grid, b, 0, st>>>(a); break;
+        case 3: ksg_grid_count_kernel<3><<<grid, b, 0, st>>>(a); break;
+        default: invalid("d must be 1, 2 or 3");
+    }
+    NSG_CUDA(cudaGetLastError());
+}
+
+void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a, const int* cnt_b,
+                         const float* psi, float* psum, int* nx, int* ny, cudaStream_t st) {
+    if (npairs <= 0) return;
+    grid_combine_kernel<<<npairs, 256, 0, st>>>(pairs, cnt_a, cnt_b, psi, psum, nx, ny);
+    NSG_CUDA(cudaGetLastError());
+}
+
+int grid_search_ctas_per_sm(int d, int kmax) {
+    int n = 0;
+    const int b = 32 * kGridWarps;
+    cudaError_t e = cudaSuccess;
+#define NSG_OCC(D_, K_) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ksg_grid_pass1_kernel<D_, K_>, b, 0)
+    switch (d * 100 + kmax) {
+        case 106: NSG_OCC(1, 6); break;
+        case 108: NSG_OCC(1, 8); break;
+        case 116: NSG_OCC(1, 16); break;
+        case 132: NSG_OCC(1, 32); break;
+        case 164: NSG_OCC(1, 64); break;
+        case 206: NSG_OCC(2, 6); break;
+        case 208: NSG_OCC(2, 8); break;
+        case 216: NSG_OCC(2, 16); break;
+        case 232: NSG_OCC(2, 32); break;
+        case 264: NSG_OCC(2, 64); break;
+        case 306: NSG_OCC(3, 6); break;
+        case 308: NSG_OCC(3, 8); break;
+        case 316: NSG_OCC(3, 16); break;
+        case 332: NSG_OCC(3, 32); break;
+        case 364: NSG_OCC(3, 64); break;
+        default: return 1;
+    }
+#undef NSG_OCC
+    cuda_check(e, "occupancy query");
+    return n > 0 ? n : 1;
+}
+
+int grid_count_ctas_per_sm(int d) {
+    int n = 0;
+    const int b = 32 * kGridWarps;
+    cudaError_t e = cudaSuccess;
+    switch (d) {
+        case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ksg_grid_count_kernel<1>, b, 0); break;
+        case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ksg_grid_count_kernel<2>, b, 0); break;
+        case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ksg_grid_count_kernel<3>, b, 0); break;
+        default: return 1;
+    }
+    cuda_check(e, "occupancy query");
+    return n > 0 ? n : 1;
+}
+
+}  // namespace nsg

@@ -1,0 +1,347 @@
+// KSG on cell grids: the same results as ksg_count_kernel with a fraction
+// of the distance evaluations.
+//
+// Every frame a query can accept lies inside an axis-aligned box around it:
+// pass 1 accepts frame j only when dz(i, j) <= the current (k+1)-th
+// distance U_i, and dz >= |fl(x_c(i) - x_c(j))| for every coordinate c;
+// pass 2 counts j only when d_a(i, j) <= eps_a(i), and d_a >= that
+// coordinate difference for every coordinate of a. So frames are grouped
+// into cells of a G x G grid over two coordinates, and a warp of 32
+// neighbouring queries visits only the cells whose bounds can reach one of
+// its queries. A cell [e_lo, e_hi) along coordinate c is skipped for query i
+// when fl(q - e_hi) > U or fl(e_lo - q) > U: rounding is monotone, so every
+// frame of the cell then has |fl(q - x)| > U. The test is exact, so the set
+// of frames a query can accept, and with it eps, the counts and every
+// output, equal the exhaustive kernel's.
+//
+// Grids:
+//   * node grid (one per trajectory row): coordinates c1, c2 with the
+//     widest spread, G-1 quantile edges on each, frames sorted by cell
+//     (cell-major over c1, then c2), coordinates copied in that order;
+//   * pair grid (one per pair and batch): cells over (c1 of a, c1 of b)
+//     with the two nodes' edges, both nodes' coordinates copied in that
+//     order with the frames' original indices.
+//
+// Warps, not CTAs, own queries: a warp takes 32 consecutive frames of the
+// pair grid (or node grid) as its queries, so their boxes overlap, and
+// streams the frames of the cells it must visit through its own slice of
+// shared memory, 128 frames at a time, read back as float4 broadcasts.
+// Pass 1 first scans the cells its queries sit in (the seed, which fills
+// the neighbour lists and bounds U), then cell rows outward from there,
+// recomputing each row's column range from the current bounds and stopping
+// in a direction at the first row no query can reach (rows further out have
+// bounds further away). The counts use the fixed eps and visit the row and
+// column ranges directly.
+#pragma once
+
+#include "common.cuh"
+#include "ksg.cuh"
+#include "ksg_grid.h"
+#include "ksg_kernels.cuh"
+
+namespace nsg {
+
+namespace gridk {
+
+__device__ __forceinline__ float inf_f() { return __int_as_float(0x7f800000); }
+
+// Edge e[t] for t in [-1, G-1]: -inf below, +inf above.
+__device__ __forceinline__ float edge_at(const float* e, int t, int G) {
+    if (t < 0) return -inf_f();
+    if (t >= G - 1) return inf_f();
+    return e[t];
+}
+
+// Can a frame of bin t (values in [e[t-1], e[t])) lie within u of q?
+__device__ __forceinline__ bool bin_reaches(const float* e, int t, int G, float q, float u) {
+    return __fsub_rn(q, edge_at(e, t, G)) <= u && __fsub_rn(edge_at(e, t - 1, G), q) <= u;
+}
+
+// Range [lo, hi] of bins that can hold frames within u of q (lo > hi: none).
+// Bins reachable form one interval: the first condition holds from some bin
+// on, the second up to some bin.
+__device__ __forceinline__ void bin_range(const float* e, int G, float q, float u, int& lo, int& hi) {
+    lo = 0;
+    while (lo < G && !(__fsub_rn(q, edge_at(e, lo, G)) <= u)) ++lo;
+    hi = G - 1;
+    while (hi >= 0 && !(__fsub_rn(edge_at(e, hi - 1, G), q) <= u)) --hi;
+}
+
+__device__ __forceinline__ int warp_min(int v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Pair index and warp block of work item t (binary search over wprefix).
+__device__ __forceinline__ void item_of(const int* wprefix, int npairs, int t, int& p, int& blk) {
+    int lo = 0, hi = npairs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(wprefix + mid) <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    p = lo;
+    blk = t - __ldg(wprefix + lo);
+}
+
+// Stage frames [base, base+n) of a sorted grid (planes of `stride` floats)
+// into this warp's tile (NP planes of kGridChunk), +inf past n; with JT also
+// their original indices.
+template <int NP, bool JT>
+__device__ __forceinline__ void stage(float* tile, int* jt, const float* sx, long long stride,
+                                      const int* perm, int base, int n, int lane) {
+#pragma unroll
+    for (int t = 0; t < kGridChunk / 32; ++t) {
+        const int f = lane + 32 * t;
+        const bool in = f < n;
+#pragma unroll
+        for (int c = 0; c < NP; ++c) {
+            tile[c * kGridChunk + f] = in ? __ldg(sx + c * stride + base + f) : inf_f();
+        }
+        if constexpr (JT) jt[f] = in ? __ldg(perm + base + f) : -1;
+    }
+}
+
+// Pass 1 over a staged chunk: frames' original indices in jt.
+template <int D, int KMAX>
+__device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, int n,
+                                            const float (&qa)[D], const float (&qb)[D],
+                                            float (&bd)[KMAX], int (&bj)[KMAX]) {
+    const int ngroups = (n + 3) >> 2;
+    for (int g = 0; g < ngroups; ++g) {
+        float4 ga[D], gb[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            ga[c] = *reinterpret_cast<const float4*>(tile + c * kGridChunk + 4 * g);
+            gb[c] = *reinterpret_cast<const float4*>(tile + (D + c) * kGridChunk + 4 * g);
+        }
+        float da[4], db[4], dz[4];
+        ksgk::Marg<D, 1>::four(qa, ga, da);
+        ksgk::Marg<D, 1>::four(qb, gb, db);
+#pragma unroll
+        for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
+        const float mn = nsg_min3(dz[0], dz[1], fminf(dz[2], dz[3]));
+        if (mn < bd[KMAX - 1]) {
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                if (dz[f] < bd[KMAX - 1]) ksgk::list_insert<KMAX>(bd, bj, dz[f], jt[4 * g + f]);
+            }
+        }
+    }
+}
+
+template <int D>
+__device__ __forceinline__ int count_chunk(const float* tile, int n, const float (&q)[D], float e) {
+    const int ngroups = (n + 3) >> 2;
+    int cnt = 0;
+    for (int g = 0; g < ngroups; ++g) {
+        float4 gq[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) gq[c] = *reinterpret_cast<const float4*>(tile + c * kGridChunk + 4 * g);
+        float dq[4];
+        ksgk::Marg<D, 1>::four(q, gq, dq);
+#pragma unroll
+        for (int f = 0; f < 4; ++f) cnt += dq[f] <= e ? 1 : 0;
+    }
+    return cnt;
+}
+
+}  // namespace gridk
+
+// ---- pass 1: joint k nearest neighbours, eps, ties -----------------------------
+template <int D, int KMAX>
+__global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_pass1_kernel(GridArgs A) {
+    using namespace gridk;
+    __shared__ __align__(16) float s_tile[kGridWarps][2 * D * kGridChunk];
+    __shared__ int s_jt[kGridWarps][kGridChunk];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    float* tile = s_tile[wid];
+    int* jt = s_jt[wid];
+    const int total = __ldg(A.wprefix + A.npairs);
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(A.counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= total) return;
+        int p, blk;
+        item_of(A.wprefix, A.npairs, t, p, blk);
+        const KsgPairDesc P = A.pairs[p];
+        const GridPair gp = A.gp[p];
+        const GridNode na = A.nodes[gp.a];
+        const GridNode nb = A.nodes[gp.b];
+        const int m = P.m, G = na.G;
+        const long long st = m;
+        const int r = blk * 32 + lane;
+        const bool valid = r < m;
+        const int i = valid ? __ldg(gp.perm + r) : 0;
+        float qa[D], qb[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            qa[c] = valid ? __ldg(gp.sx + c * st + r) : 0.f;
+            qb[c] = valid ? __ldg(gp.sx + (D + c) * st + r) : 0.f;
+        }
+        float bd[KMAX];
+        int bj[KMAX];
+        const int nsent = KMAX - (A.k + 2);
+#pragma unroll
+        for (int s = 0; s < KMAX; ++s) {
+            bd[s] = s < nsent ? -inf_f() : inf_f();
+            bj[s] = -1;
+        }
+        // cells of this warp's queries: pair cell = bin of a on c1, bin of b on c1
+        int my_cell = 0x7fffffff, my_cell_hi = -1;
+        if (valid) {
+            my_cell = (__ldg(na.cell + i) / G) * G + __ldg(nb.cell + i) / G;
+            my_cell_hi = my_cell;
+        }
+        const int cell_lo = warp_min(my_cell);
+        const int cell_hi = warp_max(my_cell_hi);
+        const int seed_lo = __ldg(gp.start + cell_lo);
+        const int seed_hi = __ldg(gp.start + cell_hi + 1);
+        auto scan = [&](int lo, int hi) {
+            for (int base = lo; base < hi; base += kGridChunk) {
+                const int n = min(kGridChunk, hi - base);
+                __syncwarp();
+                stage<2 * D, true>(tile, jt, gp.sx, st, gp.perm, base, n, lane);
+                __syncwarp();
+                pass1_chunk<D, KMAX>(tile, jt, n, qa, qb, bd, bj);
+            }
+        };
+        // ranges of a row minus the seed interval
+        auto scan_minus_seed = [&](int lo, int hi) {
+            if (hi <= lo) return;
+            if (hi <= seed_lo || lo >= seed_hi) {
+                scan(lo, hi);
+                return;
+            }
+            if (lo < seed_lo) scan(lo, seed_lo);
+            if (hi > seed_hi) scan(seed_hi, hi);
+        };
+        scan(seed_lo, seed_hi);
+        const float qa1 = qa[na.c1], qb1 = qb[nb.c1];
+        // one cell row: the column range the reaching queries need, minus the seed
+        auto do_row = [&](int cx) {
+            const float u = valid ? bd[KMAX - 1] : -inf_f();
+            const bool reach = valid && bin_reaches(na.e1, cx, G, qa1, u);
+            if (!__any_sync(0xffffffffu, reach)) return;
+            int lo = G, hi = -1;
+            if (reach) bin_range(nb.e1, G, qb1, u, lo, hi);
+            lo = warp_min(lo);
+            hi = warp_max(hi);
+            if (lo <= hi) {
+                scan_minus_seed(__ldg(gp.start + cx * G + lo), __ldg(gp.start + cx * G + hi + 1));
+            }
+        };
+        // the rows the queries sit in, then outward. Every query lies below
+        // row `up` (above row `dn`), so row `up` can only be reached across
+        // its lower edge, and if no query reaches that edge now, no row
+        // further up can be reached later (bounds only shrink).
+        const int row_first = cell_lo / G, row_last = cell_hi / G;
+        for (int cx = row_first; cx <= row_last; ++cx) do_row(cx);
+        int up = row_last + 1, dn = row_first - 1;
+        for (;;) {
+            const float u = valid ? bd[KMAX - 1] : -inf_f();
+            const bool more_up =
+                up < G && __any_sync(0xffffffffu, valid && __fsub_rn(edge_at(na.e1, up - 1, G), qa1) <= u);
+            const bool more_dn =
+                dn >= 0 && __any_sync(0xffffffffu, valid && __fsub_rn(qa1, edge_at(na.e1, dn, G)) <= u);
+            if (!more_up && !more_dn) break;
+            if (more_up) do_row(up++);
+            if (more_dn) do_row(dn--);
+        }
+        // eps from list positions 1..k (original rows), tie test
+        float ea = 0.f, eb = 0.f;
+        bool tie = false;
+        if (valid) {
+            tie = bd[KMAX - 2] == bd[KMAX - 1] && bd[KMAX - 2] > 0.f;
+#pragma unroll
+            for (int s = 1; s < KMAX - 1; ++s) {
+                const int j = bj[s];
+                if (s > nsent && j >= 0 && j < m) {
+                    ea = fmaxf(ea, ksgk::marginal_at<D>(qa, P.xa, P.ld, j));
+                    eb = fmaxf(eb, ksgk::marginal_at<D>(qb, P.xb, P.ld, j));
+                }
+            }
+            const long long o = P.scratch + i;
+            A.eps_a[o] = ea;
+            A.eps_b[o] = eb;
+            if (A.eps_x) A.eps_x[o] = ea;
+            if (A.eps_y) A.eps_y[o] = eb;
+            if (A.kdist) A.kdist[o] = bd[KMAX - 2];
+            if (tie) {
+                const int slot = atomicAdd(A.tie_count, 1);
+                if (slot < A.tie_cap) A.ties[slot] = KsgTie{A.pair_base + p, i};
+                else atomicOr(A.fault, FAULT_TIE_OVERFLOW);
+            }
+        }
+    }
+}
+
+// ---- pass 2: marginal counts on a node grid -------------------------------------
+// Work items 0 .. total-1 count variable a of each pair, total .. 2*total-1
+// variable b.
+template <int D>
+__global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArgs A) {
+    using namespace gridk;
+    __shared__ __align__(16) float s_tile[kGridWarps][D * kGridChunk];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    float* tile = s_tile[wid];
+    const int total = __ldg(A.wprefix + A.npairs);
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(A.counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= 2 * total) return;
+        const bool side_b = t >= total;
+        int p, blk;
+        item_of(A.wprefix, A.npairs, side_b ? t - total : t, p, blk);
+        const KsgPairDesc P = A.pairs[p];
+        const GridPair gp = A.gp[p];
+        const GridNode nd = A.nodes[side_b ? gp.b : gp.a];
+        const float* eps = side_b ? A.eps_b : A.eps_a;
+        int* out = side_b ? A.cnt_b : A.cnt_a;
+        const int m = P.m, G = nd.G;
+        const long long st = m;
+        const int r = blk * 32 + lane;
+        const bool valid = r < m;
+        const int i = valid ? __ldg(nd.perm + r) : 0;
+        float q[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) q[c] = valid ? __ldg(nd.sx + c * st + r) : 0.f;
+        const float e = valid ? __ldg(eps + P.scratch + i) : -inf_f();
+        const float q1 = q[nd.c1];
+        const float q2 = nd.c2 >= 0 ? q[nd.c2] : 0.f;
+        int rlo = G, rhi = -1, clo = G, chi = -1;
+        if (valid) {
+            bin_range(nd.e1, G, q1, e, rlo, rhi);
+            bin_range(nd.e2, G, q2, e, clo, chi);
+        }
+        rlo = warp_min(rlo);
+        rhi = warp_max(rhi);
+        clo = warp_min(clo);
+        chi = warp_max(chi);
+        int cnt = 0;
+        for (int cx = rlo; cx <= rhi && clo <= chi; ++cx) {
+            const int lo = __ldg(nd.start + cx * G + clo);
+            const int hi = __ldg(nd.start + cx * G + chi + 1);
+            for (int base = lo; base < hi; base += kGridChunk) {
+                const int n = min(kGridChunk, hi - base);
+                __syncwarp();
+                stage<D, false>(tile, nullptr, nd.sx, st, nullptr, base, n, lane);
+                __syncwarp();
+                cnt += count_chunk<D>(tile, n, q, e);
+            }
+        }
+        if (valid) out[P.scratch + i] = cnt;
+    }
+}
+
+}  // namespace nsg

@@ -1,0 +1,73 @@
+// Cell-grid KSG (ksg_grid.cu, ksg_grid.cuh): device descriptors and the
+// host-side launchers the planner uses.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ksg.cuh"
+
+namespace nsg {
+
+constexpr int kGridMaxG = 32;
+constexpr int kGridChunk = 128;     // frames staged per warp step
+constexpr int kGridWarps = 8;       // warps per CTA
+
+// Node grid of one trajectory row (device descriptor).
+struct GridNode {
+    const float* x;        // original row: x[c*ld + j]
+    int ld, m, G;
+    int c1, c2;            // c2 < 0 for d == 1
+    float* e1;             // kGridMaxG floats: G-1 edges along c1, then +inf
+    float* e2;             // likewise along c2 (all +inf when c2 < 0)
+    unsigned short* cell;  // [m] cell of frame j: b1*G + b2
+    int* perm;             // [m] frames in cell order
+    int* start;            // [G*G+1] first position of each cell
+    float* sx;             // [d][m] coordinates in cell order (plane stride m)
+};
+
+// Pair grid of one pair of a batch (device descriptor).
+struct GridPair {
+    int a, b;              // node indices
+    int* perm;             // [m] frames in pair-cell order
+    int* start;            // [G*G+1]
+    float* sx;             // [2d][m] coordinates of a then b in that order
+};
+
+struct GridArgs {
+    const KsgPairDesc* pairs;   // batch pairs (scratch offsets, m, out)
+    const GridPair* gp;         // same indexing as pairs
+    const GridNode* nodes;
+    const int* wprefix;         // [npairs+1] prefix of ceil(m/32) over the batch
+    int npairs;
+    int pair_base;              // index of pairs[0] in the plan's pair array (tie entries)
+    int k;
+    int* counter;
+    int* fault;
+    KsgTie* ties;
+    int* tie_count;
+    int tie_cap;
+    float* eps_a;               // scratch, per sample at pair.scratch + i
+    float* eps_b;
+    int* cnt_a;
+    int* cnt_b;
+    // optional per-sample outputs
+    float* eps_x;
+    float* eps_y;
+    float* kdist;
+};
+
+// Cells per axis for m samples (about ten frames per cell, at most kGridMaxG).
+int grid_cells_per_axis(int m);
+// Node grids (nodes: device array whose x, ld, m, G and buffers are set).
+void grid_launch_nodes(GridNode* nodes, int nnodes, int d, cudaStream_t st);
+// Pair grids of a batch (pairs, gps: device arrays of npairs).
+void grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
+                       int d, cudaStream_t st);
+void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st);
+void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st);
+void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a, const int* cnt_b,
+                         const float* psi, float* psum, int* nx, int* ny, cudaStream_t st);
+int grid_search_ctas_per_sm(int d, int kmax);
+int grid_count_ctas_per_sm(int d);
+
+}  // namespace nsg

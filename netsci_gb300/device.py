@@ -125,11 +125,13 @@ class KsgPlan:
 
     @property
     def shape(self) -> dict:
-        v = [ctypes.c_int() for _ in range(5)]
+        v = [ctypes.c_int() for _ in range(6)]
         call("nsg_ksg_plan_shape", self._h, *(ctypes.byref(x) for x in v[:4]))
         call("nsg_ksg_plan_staging", self._h, ctypes.byref(v[4]))
+        call("nsg_ksg_plan_search", self._h, ctypes.byref(v[5]))
         return dict(threads=v[0].value, r=v[1].value, frames=v[2].value, variant=v[3].value,
-                    staging="bulk-copy" if v[4].value else "loads")
+                    staging="bulk-copy" if v[4].value else "loads",
+                    search="cell-grid" if v[5].value else "exhaustive")
 
     def count_ms(self) -> float:
         """Device time (ms) of the count kernels in the last run."""
@@ -157,6 +159,11 @@ def set_ksg_shape(threads: int = 0, r: int = 0, frames: int = 0, variant: int = 
 def set_ksg_staging(staging: int = -1) -> None:
     """Tile staging for later plans: 1 bulk copies (TMA), 0 plain loads, -1 auto."""
     call("nsg_ksg_set_staging", int(staging))
+
+
+def set_ksg_search(mode: int = -1) -> None:
+    """Neighbour search for later plans: 1 cell grids, 0 exhaustive, -1 automatic."""
+    call("nsg_ksg_set_search", int(mode))
 
 
 def apsp_lengths(A: torch.Tensor, max_path_length: int, H: torch.Tensor | None = None,

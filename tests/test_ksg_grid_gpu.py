@@ -1,0 +1,105 @@
+"""Cell-grid neighbour search (ksg_grid.cuh) against the oracle: the grid
+only skips frames whose cells cannot reach a query, so every output must be
+bit-identical to the exhaustive kernel's and the reference's."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _detail(xa, xb, n, k, d):
+    from netsci_gb300 import device
+    X, m = device.pack_trajectory(np.stack([xa, xb]).reshape(2, d * n), d)
+    return device.ksg_pair_detail(X[0], X[1], m, k, d)
+
+
+@pytest.fixture
+def grid_search():
+    from netsci_gb300 import device
+    device.set_ksg_search(1)
+    yield
+    device.set_ksg_search(-1)
+
+
+@pytest.mark.parametrize("d,k,n", [(1, 4, 2500), (2, 6, 3001), (3, 6, 4096), (3, 1, 2100),
+                                   (3, 17, 2600), (2, 31, 2200), (3, 62, 2300), (3, 6, 50),
+                                   (1, 3, 9), (2, 5, 300)])
+def test_grid_matches_oracle_per_sample(oracle_mod, grid_search, d, k, n):
+    rng = np.random.default_rng(d * 1000 + k + n)
+    xa = rng.standard_normal(d * n).astype(np.float32)
+    xb = (0.6 * xa + rng.standard_normal(d * n)).astype(np.float32)
+    mi, det = oracle_mod.mi_pair(xa, xb, n, k, d, detail=True)
+    out = _detail(xa, xb, n, k, d)
+    for key in ("n_x", "n_y", "eps_x", "eps_y", "kdist"):
+        assert np.array_equal(out[key].cpu().numpy(), det[key]), key
+    assert float(out["mi"].item()) == mi
+
+
+@pytest.mark.parametrize("d,k", [(1, 4), (2, 6), (3, 6), (3, 10)])
+def test_grid_ties_follow_reference(oracle_mod, grid_search, d, k):
+    """Coarse-grid coordinates: many equal distances and equal edges."""
+    n = 2600
+    rng = np.random.default_rng(d * 31 + k)
+    xa = (np.round(rng.standard_normal(d * n) * 8) / 8).astype(np.float32)
+    xb = (np.round((0.5 * xa + rng.standard_normal(d * n)) * 8) / 8).astype(np.float32)
+    mi, det = oracle_mod.mi_pair(xa, xb, n, k, d, detail=True)
+    assert det["ties"] > 0
+    out = _detail(xa, xb, n, k, d)
+    for key in ("n_x", "n_y", "eps_x", "eps_y", "kdist"):
+        assert np.array_equal(out[key].cpu().numpy(), det[key]), key
+    assert float(out["mi"].item()) == mi
+
+
+def test_grid_plan_protein_uneven(oracle_mod):
+    """Automatic choice picks the grid for large m; pairs of several
+    trajectories with different m in one plan; graph replay."""
+    from netsci_gb300 import device, synthetic
+    pairs, expect, keep = [], [], []
+    for t, (N, m) in enumerate(((6, 2048), (5, 3333), (4, 5000))):
+        X, _ = synthetic.protein_trajectory(N, m, seed=50 + t)
+        Xd, mm = device.pack_trajectory(X, 3)
+        keep.append(Xd)
+        ab = synthetic.all_pairs(N)
+        pairs += device.make_pairs(Xd, mm, ab)
+        expect += list(oracle_mod.pairs(X, m, 3, ab, 6, gc=False, threads=8))
+    mi = torch.empty(len(pairs), device="cuda")
+    plan = device.KsgPlan(pairs, 6, 3, mi=mi, graph=True)
+    assert plan.shape["search"] == "cell-grid"
+    for _ in range(2):
+        mi.zero_()
+        plan.run()
+        torch.cuda.synchronize()
+        plan.check()
+        assert np.array_equal(mi.cpu().numpy(), np.asarray(expect, np.float32))
+
+
+def test_grid_and_exhaustive_agree_large(grid_search):
+    """m = 10000 (the large configuration's frame count): grid == exhaustive."""
+    from netsci_gb300 import device, synthetic
+    X, _ = synthetic.protein_trajectory(8, 10000, seed=81)
+    Xd, m = device.pack_trajectory(X, 3)
+    pairs = device.make_pairs(Xd, m, synthetic.all_pairs(8))
+    g = torch.empty(len(pairs), device="cuda")
+    plan = device.KsgPlan(pairs, 6, 3, gc=g)
+    assert plan.shape["search"] == "cell-grid"
+    plan.run()
+    torch.cuda.synchronize()
+    device.set_ksg_search(0)
+    e = torch.empty(len(pairs), device="cuda")
+    plan0 = device.KsgPlan(pairs, 6, 3, gc=e)
+    assert plan0.shape["search"] == "exhaustive"
+    plan0.run()
+    torch.cuda.synchronize()
+    assert np.array_equal(g.cpu().numpy(), e.cpu().numpy())
+
+
+def test_grid_refuses_frame_maps(grid_search):
+    from netsci_gb300 import NsgError, device, synthetic
+    X, _ = synthetic.protein_trajectory(3, 2500, seed=1)
+    Xd, m = device.pack_trajectory(X, 3)
+    fmap = torch.arange(m, dtype=torch.int32, device="cuda")
+    pairs = device.make_pairs(Xd, m, [[0, 1]], fmap=fmap, m_samples=m)
+    with pytest.raises(NsgError) as e:
+        device.KsgPlan(pairs, 6, 3, mi=torch.empty(1, device="cuda"))
+    assert e.value.status == 4
