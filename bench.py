@@ -19,9 +19,11 @@ Lines reported (one JSON line from rank 0):
             pair (the reference's call structure) on a small sample.
   apsp      Hedetniemi shortest-path ms on N = 2000 random geometric graphs
             (mean degree 12), integer weights U[1,100] and float weights.
-  roofline  the count kernel against the CUDA-core issue peak (SMs x 128
-            lanes x max SM clock); algorithmic work per pair
-            8*d*m*(m-1) FP32 ops.
+  roofline  the neighbour-search kernels against the CUDA-core issue peak
+            (SMs x 128 lanes x max SM clock). Work is the executed distance
+            evaluations counted by the cell-grid kernels (4d ops per joint,
+            2d per one-variable evaluation); effective_gops is the rate an
+            exhaustive search would need, 8*d*m*(m-1) ops per pair.
   cpu_baseline  the CPU oracle port (restatement of the reference CPU path)
             on all host cores, on a bounded sample of pairs of this workload.
   uneven_batch  64 trajectories of uneven N and m in one plan vs the plain
@@ -381,7 +383,20 @@ def main():
     peak_gops = props.multi_processor_count * 128 * sm_max * 1e6 / 1e9
     ops_launch = ops_per_pair(m) * B
     avg_launch_s = statistics.mean(count_ms) / 1000.0
-    achieved = ops_launch / avg_launch_s / 1e9
+    search = plans[args.warmup].shape["search"]
+    # exhaustive-equivalent rate: the work an exhaustive search needs
+    effective = ops_launch / avg_launch_s / 1e9
+    if search == "cell-grid":
+        # executed work: each joint-distance evaluation is 4d ops (2d
+        # subtractions, 2d-1 max, 1 compare), each one-variable evaluation of
+        # the counts 2d (d, d-1, 1), counted by the kernels
+        evs = [plans[s].evaluations() for s in range(args.warmup, S)]
+        exec_ops = statistics.mean(e[0] * 4 * DIM + e[1] * 2 * DIM for e in evs)
+        kernel = "ksg_grid_pass1_kernel + ksg_grid_count_kernel"
+    else:
+        exec_ops = ops_launch
+        kernel = "ksg_count_kernel"
+    achieved = exec_ops / avg_launch_s / 1e9
     clocks = clk.summary()
     frac_at_clock = None
     if clocks.get("sm_mhz"):
@@ -491,8 +506,10 @@ def main():
             "roofline": {"bound": "cuda_core_issue", "achieved": achieved,
                          "peak": peak_gops, "unit": "Gop/s", "frac": achieved / peak_gops,
                          "frac_at_median_clock": frac_at_clock, "traffic": None,
-                         "kernel": "ksg_count_kernel",
-                         "ops_per_launch": ops_launch,
+                         "kernel": kernel, "search": search,
+                         "ops_per_launch": exec_ops,
+                         "exhaustive_ops_per_launch": ops_launch,
+                         "effective_gops": effective,
                          "peak_source": (f"{props.multi_processor_count} SMs x 128 lanes x "
                                          f"{sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)")},
             "cpu_baseline": cpu, "clocks": clocks,

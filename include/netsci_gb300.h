@@ -229,6 +229,12 @@ int nsg_ksg_set_staging(int staging);
 int nsg_ksg_set_search(int mode);
 /* *mode = 1 when the plan uses cell grids, 0 when exhaustive. */
 int nsg_ksg_plan_search(const nsg_ksg_plan* plan, int* mode);
+/* Query-frame distance evaluations of the plan's last run with cell grids:
+ * joint distances of the search, one-variable distances of the counts (an
+ * exhaustive run evaluates m*m of each kind per pair). 0 for exhaustive
+ * plans. Synchronizes with the device. */
+int nsg_ksg_plan_evaluations(const nsg_ksg_plan* plan, unsigned long long* search,
+                             unsigned long long* counts);
 
 /* One pair's MI / GC without any device allocation. No counterpart in the
  * reference: it is for callers that cannot allocate device memory, such as

@@ -133,6 +133,8 @@ _SIGNATURES = {
     "nsg_ksg_plan_staging": (c_int, [c_void_p, P_int]),
     "nsg_ksg_set_search": (c_int, [c_int]),
     "nsg_ksg_plan_search": (c_int, [c_void_p, P_int]),
+    "nsg_ksg_plan_evaluations": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_ulonglong),
+                                         ctypes.POINTER(ctypes.c_ulonglong)]),
     "nsg_server_create": (c_int, [c_size_t, c_double, c_int, PP_void]),
     "nsg_server_destroy": (c_int, [c_void_p]),
     "nsg_server_register_trajectory": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, P_int]),

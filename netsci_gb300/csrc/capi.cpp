@@ -501,6 +501,14 @@ int nsg_ksg_plan_search(const nsg_ksg_plan* plan, int* mode) {
     });
 }
 
+int nsg_ksg_plan_evaluations(const nsg_ksg_plan* plan, unsigned long long* search,
+                             unsigned long long* counts) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        plan->plan->evaluations(search, counts);
+    });
+}
+
 int nsg_ksg_plan_check(nsg_ksg_plan* plan) {
     return guarded([&] {
         if (!plan || !plan->plan) nsg::invalid("plan is null");

@@ -194,15 +194,18 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
         search = g_forced_search;
     }
     bool grid_ok = npairs > 0;
-    int minm = maxm;
+    double work = 0, work_large = 0;  // sum of m^2, and over pairs with m >= kGridMinSamples
     for (const auto& q : pairs) {
         if (q.fmap) grid_ok = false;
-        minm = std::min(minm, q.m);
+        const double w = static_cast<double>(q.m) * q.m;
+        work += w;
+        if (q.m >= kGridMinSamples) work_large += w;
     }
     if (search == 1 && !grid_ok) {
         fail(NSG_ERR_UNSUPPORTED, "cell-grid search needs pairs without frame maps");
     }
-    if (search < 0) search = (grid_ok && minm >= kGridMinSamples) ? 1 : 0;
+    // automatic: grids when most of the work is in pairs large enough to prune
+    if (search < 0) search = (grid_ok && work_large >= 0.5 * work) ? 1 : 0;
     search_ = search == 1 ? 1 : 0;
 
     // ---- tile shape -----------------------------------------------------
@@ -453,6 +456,7 @@ struct KsgPlan::GridState {
     DeviceBuffer wprefix;                 // per batch: npairs+1 prefix of ceil(m/32)
     std::vector<long long> wprefix_off;   // offset of each batch's prefix
     DeviceBuffer eps_a, eps_b, cnt_a, cnt_b;
+    DeviceBuffer evals;                   // 2 counters per run (search, counts)
     int nnodes = 0;
     int search_grid = 0, count_grid = 0;
 };
@@ -561,6 +565,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
     g->eps_b.reset(ns * sizeof(float));
     g->cnt_a.reset(ns * sizeof(int));
     g->cnt_b.reset(ns * sizeof(int));
+    g->evals.reset(2 * sizeof(unsigned long long));
     g->search_grid = sm_count() * grid_search_ctas_per_sm(d_, kmax_);
     g->count_grid = sm_count() * grid_count_ctas_per_sm(d_);
     grid_ = std::move(g);
@@ -570,6 +575,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
 
 void KsgPlan::enqueue_grid(cudaStream_t s) {
     GridState& g = *grid_;
+    NSG_CUDA(cudaMemsetAsync(g.evals.get(), 0, 2 * sizeof(unsigned long long), s));
     grid_launch_nodes(g.nodes.as<GridNode>(), g.nnodes, d_, s);
     for (size_t bi = 0; bi < batches_.size(); ++bi) {
         const Batch& b = batches_[bi];
@@ -594,6 +600,7 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         a.eps_b = g.eps_b.as<float>();
         a.cnt_a = g.cnt_a.as<int>();
         a.cnt_b = g.cnt_b.as<int>();
+        a.evals = g.evals.as<unsigned long long>();
         a.eps_x = out_.eps_x;
         a.eps_y = out_.eps_y;
         a.kdist = out_.kdist;
@@ -637,6 +644,15 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
 }
 
 int KsgPlan::staging() const { return entry_ ? entry_->tma : 0; }
+
+void KsgPlan::evaluations(unsigned long long* search, unsigned long long* counts) const {
+    *search = *counts = 0;
+    if (!search_ || !grid_) return;
+    unsigned long long h[2] = {0, 0};
+    NSG_CUDA(cudaMemcpy(h, grid_->evals.get(), sizeof(h), cudaMemcpyDeviceToHost));
+    *search = h[0];
+    *counts = h[1];
+}
 
 int KsgPlan::take_fault() {
     if (!fault_.get()) return FAULT_NONE;

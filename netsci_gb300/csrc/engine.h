@@ -83,6 +83,10 @@ public:
     int variant() const { return variant_; }
     int staging() const;  // 1: bulk-copy staged kernel, 0: plain loads
     int search() const { return search_; }  // 1: cell grids, 0: exhaustive
+    // Query-frame distance evaluations of the last run's grid search (joint
+    // distances) and grid counts (one variable's distance); 0 when exhaustive.
+    // Synchronizes with the device.
+    void evaluations(unsigned long long* search, unsigned long long* counts) const;
 
 private:
     struct Batch {

@@ -58,13 +58,25 @@ __device__ __forceinline__ bool bin_reaches(const float* e, int t, int G, float 
 }
 
 // Range [lo, hi] of bins that can hold frames within u of q (lo > hi: none).
-// Bins reachable form one interval: the first condition holds from some bin
-// on, the second up to some bin.
+// Bins reachable form one interval: the first condition of bin_reaches holds
+// from some bin on (edges ascend), the second up to some bin; both bounds by
+// binary search.
 __device__ __forceinline__ void bin_range(const float* e, int G, float q, float u, int& lo, int& hi) {
-    lo = 0;
-    while (lo < G && !(__fsub_rn(q, edge_at(e, lo, G)) <= u)) ++lo;
-    hi = G - 1;
-    while (hi >= 0 && !(__fsub_rn(edge_at(e, hi - 1, G), q) <= u)) --hi;
+    int a = 0, b = G;  // first bin with fl(q - e[t]) <= u, G if none
+    while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (__fsub_rn(q, edge_at(e, mid, G)) <= u) b = mid;
+        else a = mid + 1;
+    }
+    lo = a;
+    a = 0;
+    b = G - 1;  // last bin with fl(e[t-1] - q) <= u (bin 0 always qualifies)
+    while (a < b) {
+        const int mid = (a + b + 1) >> 1;
+        if (__fsub_rn(edge_at(e, mid - 1, G), q) <= u) a = mid;
+        else b = mid - 1;
+    }
+    hi = a;
 }
 
 __device__ __forceinline__ int warp_min(int v) {
@@ -128,9 +140,22 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
         for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
         const float mn = nsg_min3(dz[0], dz[1], fminf(dz[2], dz[3]));
         if (mn < bd[KMAX - 1]) {
+            // In a pruned scan most frames are near the queries, so some lane
+            // of the warp inserts in a large share of groups. Insert each
+            // lane's nearest frame of the group first, in one shared step;
+            // it lowers the threshold, so the other frames rarely still pass.
+            int fm = 0;
+            float vm = dz[0];
+#pragma unroll
+            for (int f = 1; f < 4; ++f) {
+                const bool lt = dz[f] < vm;
+                vm = lt ? dz[f] : vm;
+                fm = lt ? f : fm;
+            }
+            ksgk::list_insert<KMAX>(bd, bj, mn, jt[4 * g + fm]);
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
-                if (dz[f] < bd[KMAX - 1]) ksgk::list_insert<KMAX>(bd, bj, dz[f], jt[4 * g + f]);
+                if (f != fm && dz[f] < bd[KMAX - 1]) ksgk::list_insert<KMAX>(bd, bj, dz[f], jt[4 * g + f]);
             }
         }
     }
@@ -156,7 +181,7 @@ __device__ __forceinline__ int count_chunk(const float* tile, int n, const float
 
 // ---- pass 1: joint k nearest neighbours, eps, ties -----------------------------
 template <int D, int KMAX>
-__global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_pass1_kernel(GridArgs A) {
+__global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid_pass1_kernel(GridArgs A) {
     using namespace gridk;
     __shared__ __align__(16) float s_tile[kGridWarps][2 * D * kGridChunk];
     __shared__ int s_jt[kGridWarps][kGridChunk];
@@ -205,7 +230,74 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_pass1_kernel(GridArg
         const int cell_hi = warp_max(my_cell_hi);
         const int seed_lo = __ldg(gp.start + cell_lo);
         const int seed_hi = __ldg(gp.start + cell_hi + 1);
-        auto scan = [&](int lo, int hi) {
+        const float qa1 = qa[na.c1], qb1 = qb[nb.c1];
+        // Ranges to scan, produced by a small state machine so that the scan
+        // body (with its unrolled list inserts) exists once in the kernel:
+        // the seed, then the rows the queries sit in, then rows outward.
+        // Every query lies below row `up` (above row `dn`), so row `up` can
+        // only be reached across its lower edge, and if no query reaches that
+        // edge now, no row further up can be reached later (bounds only
+        // shrink). A row's range minus the seed interval may leave two pieces.
+        const int row_first = cell_lo / G, row_last = cell_hi / G;
+        int phase = 0;               // 0 seed, 1 the queries' rows, 2 outward
+        int cx = row_first, up = row_last + 1, dn = row_first - 1;
+        bool prefer_up = true;
+        int pend_lo = 0, pend_hi = 0;
+        long long scanned = 0;
+        for (;;) {
+            int lo, hi;
+            if (pend_hi > pend_lo) {
+                lo = pend_lo;
+                hi = pend_hi;
+                pend_hi = pend_lo;
+            } else if (phase == 0) {
+                lo = seed_lo;
+                hi = seed_hi;
+                phase = 1;
+            } else {
+                const float u = valid ? bd[KMAX - 1] : -inf_f();
+                int row = -1;
+                if (phase == 1) {
+                    if (cx <= row_last) row = cx++;
+                    else phase = 2;
+                }
+                if (phase == 2) {
+                    const bool more_up = up < G && __any_sync(0xffffffffu, valid &&
+                        __fsub_rn(edge_at(na.e1, up - 1, G), qa1) <= u);
+                    const bool more_dn = dn >= 0 && __any_sync(0xffffffffu, valid &&
+                        __fsub_rn(qa1, edge_at(na.e1, dn, G)) <= u);
+                    if (!more_up && !more_dn) break;
+                    if (more_up && (prefer_up || !more_dn)) row = up++;
+                    else row = dn--;
+                    prefer_up = !prefer_up;
+                }
+                const bool reach = valid && bin_reaches(na.e1, row, G, qa1, u);
+                if (!__any_sync(0xffffffffu, reach)) continue;
+                int clo = G, chi = -1;
+                if (reach) bin_range(nb.e1, G, qb1, u, clo, chi);
+                clo = warp_min(clo);
+                chi = warp_max(chi);
+                if (clo > chi) continue;
+                const int ra = __ldg(gp.start + row * G + clo);
+                const int rb = __ldg(gp.start + row * G + chi + 1);
+                if (rb <= seed_lo || ra >= seed_hi) {
+                    lo = ra;
+                    hi = rb;
+                } else if (ra < seed_lo) {
+                    lo = ra;
+                    hi = seed_lo;
+                    if (rb > seed_hi) {
+                        pend_lo = seed_hi;
+                        pend_hi = rb;
+                    }
+                } else if (rb > seed_hi) {
+                    lo = seed_hi;
+                    hi = rb;
+                } else {
+                    continue;
+                }
+            }
+            scanned += hi - lo;
             for (int base = lo; base < hi; base += kGridChunk) {
                 const int n = min(kGridChunk, hi - base);
                 __syncwarp();
@@ -213,48 +305,9 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_pass1_kernel(GridArg
                 __syncwarp();
                 pass1_chunk<D, KMAX>(tile, jt, n, qa, qb, bd, bj);
             }
-        };
-        // ranges of a row minus the seed interval
-        auto scan_minus_seed = [&](int lo, int hi) {
-            if (hi <= lo) return;
-            if (hi <= seed_lo || lo >= seed_hi) {
-                scan(lo, hi);
-                return;
-            }
-            if (lo < seed_lo) scan(lo, seed_lo);
-            if (hi > seed_hi) scan(seed_hi, hi);
-        };
-        scan(seed_lo, seed_hi);
-        const float qa1 = qa[na.c1], qb1 = qb[nb.c1];
-        // one cell row: the column range the reaching queries need, minus the seed
-        auto do_row = [&](int cx) {
-            const float u = valid ? bd[KMAX - 1] : -inf_f();
-            const bool reach = valid && bin_reaches(na.e1, cx, G, qa1, u);
-            if (!__any_sync(0xffffffffu, reach)) return;
-            int lo = G, hi = -1;
-            if (reach) bin_range(nb.e1, G, qb1, u, lo, hi);
-            lo = warp_min(lo);
-            hi = warp_max(hi);
-            if (lo <= hi) {
-                scan_minus_seed(__ldg(gp.start + cx * G + lo), __ldg(gp.start + cx * G + hi + 1));
-            }
-        };
-        // the rows the queries sit in, then outward. Every query lies below
-        // row `up` (above row `dn`), so row `up` can only be reached across
-        // its lower edge, and if no query reaches that edge now, no row
-        // further up can be reached later (bounds only shrink).
-        const int row_first = cell_lo / G, row_last = cell_hi / G;
-        for (int cx = row_first; cx <= row_last; ++cx) do_row(cx);
-        int up = row_last + 1, dn = row_first - 1;
-        for (;;) {
-            const float u = valid ? bd[KMAX - 1] : -inf_f();
-            const bool more_up =
-                up < G && __any_sync(0xffffffffu, valid && __fsub_rn(edge_at(na.e1, up - 1, G), qa1) <= u);
-            const bool more_dn =
-                dn >= 0 && __any_sync(0xffffffffu, valid && __fsub_rn(qa1, edge_at(na.e1, dn, G)) <= u);
-            if (!more_up && !more_dn) break;
-            if (more_up) do_row(up++);
-            if (more_dn) do_row(dn--);
+        }
+        if (A.evals && lane == 0) {
+            atomicAdd(A.evals, static_cast<unsigned long long>(scanned) * min(32, m - blk * 32));
         }
         // eps from list positions 1..k (original rows), tie test
         float ea = 0.f, eb = 0.f;
@@ -329,9 +382,11 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
         clo = warp_min(clo);
         chi = warp_max(chi);
         int cnt = 0;
+        long long scanned = 0;
         for (int cx = rlo; cx <= rhi && clo <= chi; ++cx) {
             const int lo = __ldg(nd.start + cx * G + clo);
             const int hi = __ldg(nd.start + cx * G + chi + 1);
+            scanned += hi - lo;
             for (int base = lo; base < hi; base += kGridChunk) {
                 const int n = min(kGridChunk, hi - base);
                 __syncwarp();
@@ -341,6 +396,9 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
             }
         }
         if (valid) out[P.scratch + i] = cnt;
+        if (A.evals && lane == 0) {
+            atomicAdd(A.evals + 1, static_cast<unsigned long long>(scanned) * min(32, m - blk * 32));
+        }
     }
 }
 

@@ -50,6 +50,8 @@ struct GridArgs {
     float* eps_b;
     int* cnt_a;
     int* cnt_b;
+    // lane-frame distance evaluations done: [0] search, [1] counts
+    unsigned long long* evals;
     // optional per-sample outputs
     float* eps_x;
     float* eps_y;

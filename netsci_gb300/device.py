@@ -133,6 +133,13 @@ class KsgPlan:
                     staging="bulk-copy" if v[4].value else "loads",
                     search="cell-grid" if v[5].value else "exhaustive")
 
+    def evaluations(self) -> tuple[int, int]:
+        """(joint-distance, one-variable-distance) query-frame evaluations of
+        the last run's cell-grid search; (0, 0) for exhaustive plans."""
+        a, b = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        call("nsg_ksg_plan_evaluations", self._h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
     def count_ms(self) -> float:
         """Device time (ms) of the count kernels in the last run."""
         v = ctypes.c_float()
