@@ -35,7 +35,9 @@ struct AsyncBuffer {
 
 struct Server::Traj {
     DeviceBuffer X;
+    DeviceBuffer grid_arena;   // node grids of the rows
     int N = 0, m = 0, d = 0, ld = 0;
+    int slot0 = 0;             // node-table slot of row 0
 };
 
 struct Server::Job {
@@ -55,8 +57,11 @@ struct Server::Job {
     // device state
     AsyncBuffer dx;                  // MI rows (2 x d x ld)
     AsyncBuffer res;                 // results (one float per pair)
+    AsyncBuffer grid_arena;          // MI: node grids of the two rows
+    int mi_slot = -1;                // MI: node-table slots mi_slot, mi_slot + 1
     int ld = 0;
     std::vector<nsg_ksg_pair> pairs;
+    std::vector<std::pair<int, int>> slots;  // node-table slots of each pair's rows
     long long next_pair = 0, done_pairs = 0;
 };
 
@@ -71,6 +76,42 @@ int round_up(int v, int q) { return (v + q - 1) / q * q; }
 
 constexpr int kServeTieCtas = 32;    // 256 tie warps
 constexpr int kServeTieWarps = kServeTieCtas * 8;
+constexpr int kNodeSlots = 1 << 17;   // node-grid table entries
+constexpr int kMiSlotPairs = 4096;    // concurrent MI jobs with node grids
+constexpr int kGridTickPairs = 16384; // largest tick run on cell grids
+constexpr int kGridMinSamples = 2048;
+
+size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+// Bytes of one node's grid buffers (edges, cell starts, cells, order,
+// sorted coordinates) for m samples of d coordinates.
+size_t node_grid_bytes(int m, int d) {
+    const int G = grid_cells_per_axis(m);
+    return align16(2 * kGridMaxG * sizeof(float)) + align16((static_cast<size_t>(G) * G + 1) * sizeof(int)) +
+           align16(static_cast<size_t>(m) * sizeof(unsigned short)) + align16(static_cast<size_t>(m) * sizeof(int)) +
+           align16(static_cast<size_t>(d) * m * sizeof(float));
+}
+
+// Descriptor of a node grid whose buffers start at `base`.
+GridNode node_grid_at(unsigned char* base, const float* x, int ld, int m) {
+    GridNode n{};
+    n.x = x;
+    n.ld = ld;
+    n.m = m;
+    n.G = grid_cells_per_axis(m);
+    const size_t cells = static_cast<size_t>(n.G) * n.G + 1;
+    n.e1 = reinterpret_cast<float*>(base);
+    n.e2 = n.e1 + kGridMaxG;
+    base += align16(2 * kGridMaxG * sizeof(float));
+    n.start = reinterpret_cast<int*>(base);
+    base += align16(cells * sizeof(int));
+    n.cell = reinterpret_cast<unsigned short*>(base);
+    base += align16(static_cast<size_t>(m) * sizeof(unsigned short));
+    n.perm = reinterpret_cast<int*>(base);
+    base += align16(static_cast<size_t>(m) * sizeof(int));
+    n.sx = reinterpret_cast<float*>(base);
+    return n;
+}
 
 }  // namespace
 
@@ -98,6 +139,12 @@ Server::Server(const ServerConfig& cfg) : cfg_(cfg) {
     d_tie_idx_.reset(sizeof(int) * static_cast<size_t>(kServeTieWarps) * cfg.max_m);
     NSG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h_pairs_), sizeof(KsgPairDesc) * cap_pairs_));
     NSG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h_items_), sizeof(KsgItem) * cap_items_));
+    d_gnodes_.reset(sizeof(GridNode) * kNodeSlots);
+    d_gpairs_.reset(sizeof(GridPair) * kGridTickPairs);
+    d_wpre_.reset(sizeof(int) * (kGridTickPairs + 1));
+    NSG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h_gpairs_), sizeof(GridPair) * kGridTickPairs));
+    NSG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h_wpre_), sizeof(int) * (kGridTickPairs + 1)));
+    for (int i = kMiSlotPairs - 1; i >= 0; --i) free_mi_slots_.push_back(kNodeSlots - 2 * (i + 1));
     psi_ = device_psi(cfg.max_m);
     ksg_thread_ = std::thread([this] { ksg_loop(); });
     apsp_thread_ = std::thread([this] { apsp_loop(); });
@@ -115,6 +162,8 @@ Server::~Server() {
     trajs_.clear();
     if (h_pairs_) cudaFreeHost(h_pairs_);
     if (h_items_) cudaFreeHost(h_items_);
+    if (h_gpairs_) cudaFreeHost(h_gpairs_);
+    if (h_wpre_) cudaFreeHost(h_wpre_);
     cudaStreamDestroy(ksg_stream_);
     cudaStreamDestroy(apsp_stream_);
     cudaStreamDestroy(copy_stream_);
@@ -135,7 +184,28 @@ int Server::register_trajectory(const float* X, int N, int m, int d) {
     t->X.reset(bytes);
     NSG_CUDA(cudaMemcpy2D(t->X.get(), t->ld * sizeof(float), X, m * sizeof(float),
                           m * sizeof(float), static_cast<size_t>(N) * d, cudaMemcpyHostToDevice));
-    used_bytes_ += bytes;
+    // node grids of every row, built once: the cell-grid search of later ticks reads them
+    size_t gbytes = 0;
+    if (next_node_slot_ + N <= kNodeSlots - 2 * kMiSlotPairs) {
+        const size_t per = node_grid_bytes(m, d);
+        gbytes = per * N;
+        t->grid_arena.reset(gbytes);
+        t->slot0 = next_node_slot_;
+        std::vector<GridNode> nodes(N);
+        const size_t row = static_cast<size_t>(d) * t->ld;
+        for (int a = 0; a < N; ++a) {
+            nodes[a] = node_grid_at(t->grid_arena.as<unsigned char>() + per * a, t->X.as<float>() + a * row,
+                                    t->ld, m);
+        }
+        GridNode* dst = d_gnodes_.as<GridNode>() + t->slot0;
+        NSG_CUDA(cudaMemcpy(dst, nodes.data(), sizeof(GridNode) * N, cudaMemcpyHostToDevice));
+        grid_launch_nodes(dst, N, d, nullptr);
+        NSG_CUDA(cudaDeviceSynchronize());
+        next_node_slot_ += N;
+    } else {
+        t->slot0 = -1;  // node table full: this trajectory runs the exhaustive search
+    }
+    used_bytes_ += bytes + gbytes;
     peak_bytes_ = std::max(peak_bytes_, used_bytes_);
     trajs_.push_back(std::move(t));
     return static_cast<int>(trajs_.size()) - 1;
@@ -257,11 +327,14 @@ bool Server::try_admit_locked(Job& j) {
         const long long P = static_cast<long long>(T.N) * (T.N - 1) / 2;
         j.res.alloc(sizeof(float) * std::max<long long>(P, 1), ksg_stream_);
         j.pairs.reserve(P);
+        j.slots.reserve(T.slot0 >= 0 ? P : 0);
         const size_t row = static_cast<size_t>(T.d) * T.ld;
         for (int a = 0; a < T.N; ++a)
-            for (int b = a + 1; b < T.N; ++b)
+            for (int b = a + 1; b < T.N; ++b) {
                 j.pairs.push_back({T.X.as<float>() + a * row, T.X.as<float>() + b * row, nullptr,
                                    T.ld, T.m});
+                if (T.slot0 >= 0) j.slots.push_back({T.slot0 + a, T.slot0 + b});
+            }
     } else {
         j.dx.alloc(sizeof(float) * 2 * static_cast<size_t>(j.d) * j.ld, ksg_stream_);
         j.res.alloc(sizeof(float), ksg_stream_);
@@ -272,6 +345,22 @@ bool Server::try_admit_locked(Job& j) {
                                    j.n * sizeof(float), j.d, cudaMemcpyHostToDevice, ksg_stream_));
         j.pairs.push_back({j.dx.as<float>(), j.dx.as<float>() + static_cast<size_t>(j.d) * j.ld,
                            nullptr, j.ld, j.n});
+        if (!free_mi_slots_.empty()) {
+            j.mi_slot = free_mi_slots_.back();
+            free_mi_slots_.pop_back();
+            const size_t per = node_grid_bytes(j.n, j.d);
+            j.grid_arena.alloc(2 * per, ksg_stream_);
+            GridNode nodes[2];
+            for (int r = 0; r < 2; ++r) {
+                nodes[r] = node_grid_at(j.grid_arena.as<unsigned char>() + per * r,
+                                        j.dx.as<float>() + static_cast<size_t>(r) * j.d * j.ld, j.ld, j.n);
+            }
+            GridNode* dst = d_gnodes_.as<GridNode>() + j.mi_slot;
+            NSG_CUDA(cudaMemcpyAsync(dst, nodes, sizeof(nodes), cudaMemcpyHostToDevice, ksg_stream_));
+            NSG_CUDA(cudaStreamSynchronize(ksg_stream_));  // the host descriptors go out of scope
+            grid_launch_nodes(dst, 2, j.d, ksg_stream_);
+            j.slots.push_back({j.mi_slot, j.mi_slot + 1});
+        }
     }
     j.state = JOB_RUNNING;
     j.t.admit = now();
@@ -281,15 +370,163 @@ bool Server::try_admit_locked(Job& j) {
 void Server::release_locked(Job& j) {
     j.dx.release();
     j.res.release();
+    j.grid_arena.release();
+    if (j.mi_slot >= 0) free_mi_slots_.push_back(j.mi_slot);
+    j.mi_slot = -1;
     j.pairs.clear();
     j.pairs.shrink_to_fit();
+    j.slots.clear();
+    j.slots.shrink_to_fit();
     if (j.admitted) used_bytes_ -= j.footprint;
     j.admitted = false;
 }
 
 // One tick over the given job slices (all of one (d, KMAX) group).
+// A tick on cell grids when its pairs have node grids and most of its work
+// is in pairs with m >= kGridMinSamples; false: the caller runs the
+// exhaustive kernel.
+bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long long>>>& slices) {
+    const int d = slices[0].first->d;
+    const int k = slices[0].first->k;
+    const int kmax = ksg_kmax_for(k);
+    long long np = 0;
+    double work = 0, work_large = 0;
+    for (auto& sl : slices) {
+        Job* j = sl.first;
+        const long long cnt = sl.second.second - sl.second.first;
+        if (static_cast<long long>(j->slots.size()) != static_cast<long long>(j->pairs.size())) return false;
+        np += cnt;
+        const double w = static_cast<double>(j->n) * j->n * cnt;
+        work += w;
+        if (j->n >= kGridMinSamples) work_large += w;
+    }
+    if (np > kGridTickPairs || work_large < 0.5 * work) return false;
+
+    // descriptors, pair-grid arena offsets, warp-block prefix
+    long long samples = 0, wacc = 0;
+    size_t arena = 0;
+    long long p = 0;
+    std::vector<long long> slice_first(slices.size());
+    for (size_t si = 0; si < slices.size(); ++si) {
+        Job* j = slices[si].first;
+        slice_first[si] = p;
+        for (long long q = slices[si].second.first; q < slices[si].second.second; ++q, ++p) {
+            const nsg_ksg_pair& pr = j->pairs[q];
+            KsgPairDesc& dd = h_pairs_[p];
+            dd.xa = pr.xa;
+            dd.xb = pr.xb;
+            dd.fmap = nullptr;
+            dd.ld = pr.ld;
+            dd.m = pr.m;
+            dd.out = static_cast<int>(q);
+            dd.pad = 0;
+            dd.scratch = samples;
+            samples += pr.m;
+            GridPair& g = h_gpairs_[p];
+            g.a = j->slots[q].first;
+            g.b = j->slots[q].second;
+            const int G = grid_cells_per_axis(pr.m);
+            g.start = reinterpret_cast<int*>(arena);
+            arena += align16((static_cast<size_t>(G) * G + 1) * sizeof(int));
+            g.perm = reinterpret_cast<int*>(arena);
+            arena += align16(static_cast<size_t>(pr.m) * sizeof(int));
+            g.sx = reinterpret_cast<float*>(arena);
+            arena += align16(static_cast<size_t>(2 * d) * pr.m * sizeof(float));
+            h_wpre_[p] = static_cast<int>(wacc);
+            wacc += (pr.m + 31) / 32;
+        }
+    }
+    h_wpre_[np] = static_cast<int>(wacc);
+    cudaStream_t s = ksg_stream_;
+    // buffers grow on demand (by a quarter more than asked, to grow rarely)
+    auto ensure = [&](DeviceBuffer& b, size_t bytes) {
+        if (b.bytes() < bytes) {
+            NSG_CUDA(cudaStreamSynchronize(s));
+            b.reset(bytes + bytes / 4);
+        }
+    };
+    ensure(d_garena_, std::max<size_t>(arena, 16));
+    ensure(d_eps_a_, sizeof(float) * samples);
+    ensure(d_eps_b_, sizeof(float) * samples);
+    ensure(d_cnt_a_, sizeof(int) * samples);
+    ensure(d_cnt_b_, sizeof(int) * samples);
+    const uintptr_t base = reinterpret_cast<uintptr_t>(d_garena_.get());
+    for (long long i = 0; i < np; ++i) {
+        GridPair& g = h_gpairs_[i];
+        g.start = reinterpret_cast<int*>(base + reinterpret_cast<uintptr_t>(g.start));
+        g.perm = reinterpret_cast<int*>(base + reinterpret_cast<uintptr_t>(g.perm));
+        g.sx = reinterpret_cast<float*>(base + reinterpret_cast<uintptr_t>(g.sx));
+    }
+    NSG_CUDA(cudaMemcpyAsync(d_pairs_.get(), h_pairs_, sizeof(KsgPairDesc) * np, cudaMemcpyHostToDevice, s));
+    NSG_CUDA(cudaMemcpyAsync(d_gpairs_.get(), h_gpairs_, sizeof(GridPair) * np, cudaMemcpyHostToDevice, s));
+    NSG_CUDA(cudaMemcpyAsync(d_wpre_.get(), h_wpre_, sizeof(int) * (np + 1), cudaMemcpyHostToDevice, s));
+    NSG_CUDA(cudaMemsetAsync(d_counters_.get(), 0, sizeof(int) * 4, s));
+    int* ctr = d_counters_.as<int>();
+    KsgPairDesc* dp = d_pairs_.as<KsgPairDesc>();
+    grid_launch_pairs(dp, d_gpairs_.as<GridPair>(), d_gnodes_.as<GridNode>(), static_cast<int>(np), d, s);
+    GridArgs a{};
+    a.pairs = dp;
+    a.gp = d_gpairs_.as<GridPair>();
+    a.nodes = d_gnodes_.as<GridNode>();
+    a.wprefix = d_wpre_.as<int>();
+    a.npairs = static_cast<int>(np);
+    a.pair_base = 0;
+    a.k = k;
+    a.counter = ctr;
+    a.fault = d_fault_.as<int>();
+    a.ties = d_ties_.as<KsgTie>();
+    a.tie_count = ctr + 2;
+    a.tie_cap = tie_cap_;
+    a.eps_a = d_eps_a_.as<float>();
+    a.eps_b = d_eps_b_.as<float>();
+    a.cnt_a = d_cnt_a_.as<int>();
+    a.cnt_b = d_cnt_b_.as<int>();
+    const int sms = sm_count();
+    grid_launch_search(a, d, kmax, sms * grid_search_ctas_per_sm(d, kmax), s);
+    a.counter = ctr + 1;
+    grid_launch_counts(a, d, sms * grid_count_ctas_per_sm(d), s);
+    grid_launch_combine(dp, static_cast<int>(np), a.cnt_a, a.cnt_b, psi_->as<float>(), d_scratch_.as<float>(),
+                        nullptr, nullptr, s);
+    KsgTieArgs t{};
+    t.pairs = dp;
+    t.ties = a.ties;
+    t.tie_count = ctr + 2;
+    t.tie_cap = tie_cap_;
+    t.tie_next = ctr + 3;
+    t.k = k;
+    t.fault = a.fault;
+    t.psi = psi_->as<float>();
+    t.psum = d_scratch_.as<float>();
+    t.dz = d_tie_dz_.as<float>();
+    t.idx = d_tie_idx_.as<int>();
+    t.stride = cfg_.max_m;
+    ksg_launch_ties_ctas(t, d, kServeTieCtas, s);
+    for (size_t si = 0; si < slices.size(); ++si) {
+        Job* j = slices[si].first;
+        KsgFinalArgs f{};
+        f.pairs = dp + slice_first[si];
+        f.npairs = static_cast<int>(slices[si].second.second - slices[si].second.first);
+        f.k = k;
+        f.d = d;
+        f.psi = psi_->as<float>();
+        f.psum = d_scratch_.as<float>();
+        if (j->kind == JOB_GC) f.gc = j->res.as<float>();
+        else f.mi = j->res.as<float>();
+        ksg_launch_final(f, s);
+    }
+    NSG_CUDA(cudaStreamSynchronize(s));
+    int fault = 0;
+    NSG_CUDA(cudaMemcpy(&fault, d_fault_.get(), sizeof(int), cudaMemcpyDeviceToHost));
+    if (fault) {
+        NSG_CUDA(cudaMemset(d_fault_.get(), 0, sizeof(int)));
+        raise_fault(fault);
+    }
+    return true;
+}
+
 void Server::run_tick(std::vector<std::pair<Job*, std::pair<long long, long long>>>& slices) {
     if (slices.empty()) return;
+    if (run_tick_grid(slices)) return;
     const int d = slices[0].first->d;
     const int k = slices[0].first->k;
     const int kmax = ksg_kmax_for(k);
@@ -423,7 +660,9 @@ void Server::ksg_loop() {
                     Job& j = *active[i];
                     const long long remaining = static_cast<long long>(j.pairs.size()) - j.next_pair - take[i];
                     if (remaining <= 0) continue;
-                    const double per = 8.0 * j.d * j.n * (j.n - 1.0);
+                    // a pair's work; pairs searched on cell grids evaluate about 40% of it
+                    const double per = 8.0 * j.d * j.n * (j.n - 1.0) *
+                                       (j.slots.size() == j.pairs.size() && j.n >= kGridMinSamples ? 0.4 : 1.0);
                     const double budget = pass == 0 ? share : cfg_.tick_ops - used_ops;
                     long long t = std::max<long long>(1, static_cast<long long>(budget / per));
                     t = std::min(t, remaining);

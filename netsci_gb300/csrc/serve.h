@@ -25,6 +25,7 @@
 
 #include "engine.h"
 #include "ksg.cuh"
+#include "ksg_grid.h"
 
 namespace nsg {
 
@@ -74,6 +75,7 @@ private:
     bool try_admit_locked(Job& j);
     void release_locked(Job& j);
     void run_tick(std::vector<std::pair<Job*, std::pair<long long, long long>>>& slices);
+    bool run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long long>>>& slices);
     double now() const;
 
     ServerConfig cfg_;
@@ -97,6 +99,14 @@ private:
     int tie_cap_ = 0;
     KsgPairDesc* h_pairs_ = nullptr;
     KsgItem* h_items_ = nullptr;
+    // cell-grid search: one device table of node grids (trajectory rows from
+    // the bottom, pairs of slots for MI jobs from a free list at the top),
+    // and per-tick pair grids and scratch, grown on demand
+    DeviceBuffer d_gnodes_, d_gpairs_, d_wpre_, d_garena_, d_eps_a_, d_eps_b_, d_cnt_a_, d_cnt_b_;
+    GridPair* h_gpairs_ = nullptr;
+    int* h_wpre_ = nullptr;
+    int next_node_slot_ = 0;
+    std::vector<int> free_mi_slots_;
     std::shared_ptr<const DeviceBuffer> psi_;
     std::thread ksg_thread_, apsp_thread_;
 };

@@ -51,3 +51,34 @@ def test_server_one_job_each_kind_and_budget():
     assert float(mi[0]) == oracle.mi_pair(x, y, 1500, 4, 1)
     Ho, _, _ = oracle.apsp_lengths(A, 150)
     assert np.array_equal(H, Ho)
+
+
+def test_grid_ticks_match_plans():
+    """Jobs large enough for the cell-grid search (m >= 2048) share ticks
+    with each other and with a small job; every result equals the same job
+    run alone through a plan."""
+    import torch
+    from netsci_gb300 import device, serving, synthetic
+    X1, _ = synthetic.protein_trajectory(6, 3000, seed=21)
+    X2, _ = synthetic.protein_trajectory(5, 2500, seed=22)
+    X3, _ = synthetic.protein_trajectory(4, 600, seed=23)
+    x, y = synthetic.gaussian_pair(4000, 0.5, seed=24)
+
+    def alone_gc(X):
+        Xd, m = device.pack_trajectory(X, 3)
+        pairs = device.make_pairs(Xd, m, synthetic.all_pairs(X.shape[0]))
+        g = torch.empty(len(pairs), device="cuda")
+        device.ksg_pairs(pairs, 6, 3, gc=g)
+        return g.cpu().numpy()
+
+    with serving.Server(budget_bytes=4 << 30, tick_ops=5e9) as srv:
+        ts = [srv.register_trajectory(X, 3) for X in (X1, X2, X3)]
+        jobs = [srv.submit_gc(t, X.shape[0], 6) for t, X in zip(ts, (X1, X2, X3))]
+        jm = srv.submit_mi(x, y, 1, 4)
+        got = [srv.wait(j) for j in jobs]
+        mi = srv.wait(jm)
+        assert srv.stats()["ticks"] >= 2
+    for g, X in zip(got, (X1, X2, X3)):
+        assert np.array_equal(g, alone_gc(X))
+    import oracle
+    assert float(mi[0]) == oracle.mi_pair(x, y, 4000, 4, 1)
