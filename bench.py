@@ -312,7 +312,7 @@ def main():
 
     import torch
     import torch.distributed as dist
-    from netsci_gb300 import device, synthetic
+    from netsci_gb300 import device, sharding, synthetic
 
     torch.cuda.set_device(local)
     if world > 1:
@@ -323,17 +323,13 @@ def main():
             dist.barrier()
 
     def max_over_ranks(v: float) -> float:
-        if world == 1:
-            return v
-        t = torch.tensor([v], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return sharding.max_over_ranks(v, device="cuda")
 
     X, mean, N, m = workload(args.quick)
     ab_all = synthetic.all_pairs(N)
     B = args.pairs_per_step
     S = args.warmup + args.steps
-    need = world * S * B
+    need = sharding.pairs_needed(world, S, B)
     if need > len(ab_all):
         raise SystemExit(f"{need} pairs requested, the workload has {len(ab_all)}")
 
@@ -341,8 +337,7 @@ def main():
     torch.cuda.synchronize()
 
     def slice_for(step: int) -> np.ndarray:
-        off = (rank * S + step) * B
-        return ab_all[off:off + B]
+        return sharding.rank_batch(ab_all, rank, S, step, B)
 
     # ---- batched persistent plans (graph + kernel events) --------------------
     outs, plans = [], []
@@ -368,7 +363,7 @@ def main():
     count_ms = [plans[s].count_ms() for s in range(args.warmup, S)]
     launches = sum(plans[s].launches for s in range(args.warmup, S))
     t_max = max_over_ranks(dev_ms) / 1000.0
-    value = world * args.steps * B / t_max
+    value = sharding.weak_scaling_value(world, args.steps, B, t_max)
     gc_vals = torch.cat([outs[s] for s in range(args.warmup, S)]).cpu().numpy()
     assert np.all(np.isfinite(gc_vals)) and np.all((gc_vals >= 0) & (gc_vals <= 1))
 
