@@ -53,6 +53,11 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "netsci_gb300" / "dropin"))
 
 N_NODES, M_FRAMES, DIM, K_NN = 2000, 10000, 3, 6
+# DRAM bytes per pair of the search + count kernels at m = 10000, from an ncu
+# capture of a 256-pair step of this workload (profiles/ksg_grid_kernels_N2000_m10000.md:
+# pass 1 109.0 MB read + 13.6 MB written, counts 63.0 + 6.9 MB); the traffic
+# is per pair (each pair's grid copies and rows), so it scales with the pairs.
+GRID_DRAM_BYTES_PER_PAIR = (109.0 + 13.6 + 63.0 + 6.9) * 1e6 / 256
 SEED = 2000
 METRIC = "GC pairs/sec (batched persistent), N=2000 nodes, m=10000 frames"
 
@@ -388,9 +393,11 @@ def main():
         evs = [plans[s].evaluations() for s in range(args.warmup, S)]
         exec_ops = statistics.mean(e[0] * 4 * DIM + e[1] * 2 * DIM for e in evs)
         kernel = "ksg_grid_pass1_kernel + ksg_grid_count_kernel"
+        traffic = GRID_DRAM_BYTES_PER_PAIR * B if m == M_FRAMES else None
     else:
         exec_ops = ops_launch
         kernel = "ksg_count_kernel"
+        traffic = None
     achieved = exec_ops / avg_launch_s / 1e9
     clocks = clk.summary()
     frac_at_clock = None
@@ -500,7 +507,9 @@ def main():
             "gpu_launches": launches,
             "roofline": {"bound": "cuda_core_issue", "achieved": achieved,
                          "peak": peak_gops, "unit": "Gop/s", "frac": achieved / peak_gops,
-                         "frac_at_median_clock": frac_at_clock, "traffic": None,
+                         "frac_at_median_clock": frac_at_clock, "traffic": traffic,
+                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
+                                            "256-pair step, scaled by pairs" if traffic else None),
                          "kernel": kernel, "search": search,
                          "ops_per_launch": exec_ops,
                          "exhaustive_ops_per_launch": ops_launch,
