@@ -224,8 +224,8 @@ int nsg_ksg_set_shape(int threads, int r, int frames, int variant);
 int nsg_ksg_set_staging(int staging);
 /* Search for later plans: 1 cell grids (ksg_grid.cuh: only the frames whose
  * cells can reach a query are evaluated; same results), 0 exhaustive, -1
- * automatic (cell grids when no pair has a frame map and every pair has at
- * least 2048 samples). */
+ * automatic (cell grids when no pair has a frame map and at least half of
+ * the work, counted as m^2 per pair, is in pairs with m >= 1000). */
 int nsg_ksg_set_search(int mode);
 /* *mode = 1 when the plan uses cell grids, 0 when exhaustive. */
 int nsg_ksg_plan_search(const nsg_ksg_plan* plan, int* mode);

@@ -76,8 +76,9 @@ int g_forced_variant = -1;
 int g_forced_staging = -1;
 int g_forced_search = -1;
 // Below this many samples per pair the exhaustive kernel is used: grids of
-// a few cells per axis prune little.
-constexpr int kGridMinSamples = 2048;
+// a few cells per axis prune little (measured: 0.91x at m = 300, 1.08x at
+// m = 1000, 1.28x at m = 2000, whole plans of 48-node trajectories).
+constexpr int kGridMinSamples = 1000;
 // per batch: work-queue heads (two for the grid search), tie count, tie-kernel counter
 constexpr int kCounters = 4;
 }  // namespace

@@ -79,7 +79,7 @@ constexpr int kServeTieWarps = kServeTieCtas * 8;
 constexpr int kNodeSlots = 1 << 17;   // node-grid table entries
 constexpr int kMiSlotPairs = 4096;    // concurrent MI jobs with node grids
 constexpr int kGridTickPairs = 16384; // largest tick run on cell grids
-constexpr int kGridMinSamples = 2048;
+constexpr int kGridMinSamples = 1000;
 
 size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
