@@ -190,10 +190,14 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
 
     // ---- search: cell grids when every pair allows them -------------------
     int search = opt.search;
-    if (search < 0) {
+    bool tile_forced = opt.shape.threads != 0 || opt.staging == 1;
+    {
         std::lock_guard<std::mutex> lk(g_shape_mu);
-        search = g_forced_search;
+        if (search < 0) search = g_forced_search;
+        tile_forced = tile_forced || g_forced.threads != 0 || g_forced_staging == 1;
     }
+    // a forced tile shape or bulk-copy staging asks for the exhaustive kernel
+    if (search < 0 && tile_forced) search = 0;
     bool grid_ok = npairs > 0;
     double work = 0, work_large = 0;  // sum of m^2, and over pairs with m >= kGridMinSamples
     for (const auto& q : pairs) {
