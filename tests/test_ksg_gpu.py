@@ -154,7 +154,9 @@ def test_protein56_device_plan_graph(golden, oracle_mod):
         plan.run()
         torch.cuda.synchronize()
         assert np.array_equal(gc.cpu().numpy(), g1)
-    assert plan.launches == 3
+    # exhaustive: count, ties, finalize; cell grids (m = 1000 selects them):
+    # node grids, pair grids, search, counts, combine, ties, finalize
+    assert plan.launches == (7 if plan.shape["search"] == "cell-grid" else 3)
 
 
 def test_uneven_trajectories_one_plan(oracle_mod):
