@@ -164,17 +164,17 @@ long long count_items(const std::vector<nsg_ksg_pair>& pairs, int qc) {
 
 }  // namespace
 
-KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const KsgOutputs& out,
+KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const KsgOutputs& out,
                  const KsgPlanOptions& opt)
     : d_(d), k_(k), kmax_(ksg_kmax_for(k)), timing_(opt.timing), out_(out), graph_(opt.graph) {
     if (d < 1 || d > 3) invalid("d must be 1, 2 or 3 (got " + std::to_string(d) + ")");
     if (k < 1) invalid("k must be >= 1");
-    const int npairs = static_cast<int>(pairs.size());
+    const int npairs = static_cast<int>(pairs_in.size());
     npairs_ = npairs;
     int maxm = 0;
     long long total_samples = 0;
     for (int p = 0; p < npairs; ++p) {
-        const auto& q = pairs[p];
+        const auto& q = pairs_in[p];
         if (!q.xa || !q.xb) invalid("pair " + std::to_string(p) + " has a null row pointer");
         if (q.m < k + 1) {
             invalid("pair " + std::to_string(p) + ": k must be smaller than the number of samples (k=" +
@@ -198,20 +198,64 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
     }
     // a forced tile shape or bulk-copy staging asks for the exhaustive kernel
     if (search < 0 && tile_forced) search = 0;
-    bool grid_ok = npairs > 0;
+    // Frame-mapped rows (bootstrap resamples) are copied out once per run for
+    // the cell-grid search: one copy per distinct (row, map).
+    struct RowKey {
+        const float* x;
+        const int* fmap;
+        int m, ld;
+        bool operator<(const RowKey& o) const {
+            if (x != o.x) return x < o.x;
+            if (fmap != o.fmap) return fmap < o.fmap;
+            if (m != o.m) return m < o.m;
+            return ld < o.ld;
+        }
+    };
+    std::map<RowKey, size_t> mapped;  // row -> offset (floats) of its copy
+    size_t mapped_floats = 0;
     double work = 0, work_large = 0;  // sum of m^2, and over pairs with m >= kGridMinSamples
-    for (const auto& q : pairs) {
-        if (q.fmap) grid_ok = false;
+    for (const auto& q : pairs_in) {
         const double w = static_cast<double>(q.m) * q.m;
         work += w;
         if (q.m >= kGridMinSamples) work_large += w;
+        if (!q.fmap) continue;
+        for (const float* x : {q.xa, q.xb}) {
+            if (mapped.emplace(RowKey{x, q.fmap, q.m, q.ld}, mapped_floats).second) {
+                mapped_floats += static_cast<size_t>(d) * ((q.m + 63) / 64 * 64);
+            }
+        }
     }
+    const bool grid_ok = npairs > 0 && mapped_floats * sizeof(float) <= (size_t(8) << 30);
     if (search == 1 && !grid_ok) {
-        fail(NSG_ERR_UNSUPPORTED, "cell-grid search needs pairs without frame maps");
+        fail(NSG_ERR_UNSUPPORTED, "cell-grid search: copies of the frame-mapped rows exceed 8 GiB");
     }
     // automatic: grids when most of the work is in pairs large enough to prune
     if (search < 0) search = (grid_ok && work_large >= 0.5 * work) ? 1 : 0;
     search_ = search == 1 ? 1 : 0;
+    std::vector<nsg_ksg_pair> eff;
+    if (search_ && !mapped.empty()) {
+        mapped_rows_.reset(mapped_floats * sizeof(float));
+        std::vector<GatherRow> rows;
+        for (const auto& kv : mapped) {
+            rows.push_back({kv.first.x, kv.first.fmap, mapped_rows_.as<float>() + kv.second, kv.first.ld,
+                            kv.first.m, (kv.first.m + 63) / 64 * 64});
+        }
+        gather_rows_.reset(rows.size() * sizeof(GatherRow));
+        NSG_CUDA(cudaMemcpy(gather_rows_.get(), rows.data(), rows.size() * sizeof(GatherRow),
+                            cudaMemcpyHostToDevice));
+        ngather_ = static_cast<int>(rows.size());
+        eff = pairs_in;
+        for (auto& q : eff) {
+            if (!q.fmap) continue;
+            const int ld_out = (q.m + 63) / 64 * 64;
+            q.xa = mapped_rows_.as<float>() + mapped.at(RowKey{q.xa, q.fmap, q.m, q.ld});
+            q.xb = mapped_rows_.as<float>() + mapped.at(RowKey{q.xb, q.fmap, q.m, q.ld});
+            q.fmap = nullptr;
+            q.ld = ld_out;
+        }
+        bootstrap_ = true;
+    }
+    const std::vector<nsg_ksg_pair>& pairs = eff.empty() ? pairs_in : eff;
 
     // ---- tile shape -----------------------------------------------------
     // explicit per-plan shape, then the process-wide override, then the
@@ -367,8 +411,10 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs, int k, int d, const Ksg
             for (int p = b.pair0; p < b.pair0 + b.npairs; ++p) sum += descs[p].m;
             batch_samples = std::max(batch_samples, sum);
         }
+        // copies of resampled frames tie on many samples; on cell grids they
+        // are all listed (the tie kernel sets the harmless ones aside)
         tie_cap_ = static_cast<int>(std::min<long long>(
-            std::max<long long>(65536, batch_samples / 4), 1LL << 30));
+            std::max<long long>(65536, bootstrap_ ? batch_samples : batch_samples / 4), 1LL << 30));
         ties_.reset(static_cast<size_t>(tie_cap_) * sizeof(KsgTie));
         tie_stride_ = maxm;
         tie_dz_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(float));
@@ -581,6 +627,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
 void KsgPlan::enqueue_grid(cudaStream_t s) {
     GridState& g = *grid_;
     NSG_CUDA(cudaMemsetAsync(g.evals.get(), 0, 2 * sizeof(unsigned long long), s));
+    grid_launch_gather(gather_rows_.as<GatherRow>(), ngather_, d_, fault_.as<int>(), s);
     grid_launch_nodes(g.nodes.as<GridNode>(), g.nnodes, d_, s);
     for (size_t bi = 0; bi < batches_.size(); ++bi) {
         const Batch& b = batches_[bi];
@@ -633,6 +680,8 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         t.dz = tie_dz_.as<float>();
         t.idx = tie_idx_.as<int>();
         t.stride = tie_stride_;
+        t.gp = g.gps.as<GridPair>();
+        t.nodes = g.nodes.as<GridNode>();
         ksg_launch_ties(t, d_, s);
         KsgFinalArgs f{};
         f.pairs = bp;

@@ -72,7 +72,7 @@ public:
     // combine, ties and finalize per batch (cell-grid search).
     int launches() const {
         const int nb = static_cast<int>(batches_.size());
-        return search_ == 1 ? (nb ? 1 + 6 * nb : 0) : 3 * nb;
+        return search_ == 1 ? (nb ? 1 + (ngather_ ? 1 : 0) + 6 * nb : 0) : 3 * nb;
     }
     // Device time of the count kernels of the last run (ms); needs timing.
     float count_ms() const;
@@ -112,6 +112,9 @@ private:
     int tie_cap_ = 0;
     long long tie_stride_ = 0;
     int search_ = 0;
+    bool bootstrap_ = false;             // frame-mapped rows copied for the grid search
+    DeviceBuffer mapped_rows_, gather_rows_;
+    int ngather_ = 0;
     struct GridState;
     std::shared_ptr<GridState> grid_;
     std::shared_ptr<const DeviceBuffer> psi_;

@@ -195,6 +195,26 @@ __global__ void grid_combine_kernel(const KsgPairDesc* pairs, const int* cnt_a, 
     }
 }
 
+// One CTA per row.
+__global__ void grid_gather_kernel(const GatherRow* rows, int d, int* fault) {
+    const GatherRow g = rows[blockIdx.x];
+    const float inf = __int_as_float(0x7f800000);
+    for (int s = threadIdx.x; s < g.ld_out; s += blockDim.x) {
+        int f = 0;
+        if (s < g.m) {
+            f = __ldg(g.fmap + s);
+            if (f < 0 || f >= g.ld) {
+                atomicOr(fault, FAULT_BAD_INDEX);
+                f = 0;
+            }
+        }
+        for (int c = 0; c < d; ++c) {
+            g.out[static_cast<long long>(c) * g.ld_out + s] =
+                s < g.m ? __ldg(g.x + static_cast<long long>(c) * g.ld + f) : inf;
+        }
+    }
+}
+
 template <int D>
 void launch_pass1(const GridArgs& a, int kmax, int grid, cudaStream_t st) {
     const dim3 b(32 * kGridWarps);
@@ -264,6 +284,12 @@ void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a,
                          const float* psi, float* psum, int* nx, int* ny, cudaStream_t st) {
     if (npairs <= 0) return;
     grid_combine_kernel<<<npairs, 256, 0, st>>>(pairs, cnt_a, cnt_b, psi, psum, nx, ny);
+    NSG_CUDA(cudaGetLastError());
+}
+
+void grid_launch_gather(const GatherRow* rows, int nrows, int d, int* fault, cudaStream_t st) {
+    if (nrows <= 0) return;
+    grid_gather_kernel<<<nrows, 256, 0, st>>>(rows, d, fault);
     NSG_CUDA(cudaGetLastError());
 }
 

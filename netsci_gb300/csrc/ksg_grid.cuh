@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
             if (A.kdist) A.kdist[o] = bd[KMAX - 2];
             if (tie) {
                 const int slot = atomicAdd(A.tie_count, 1);
-                if (slot < A.tie_cap) A.ties[slot] = KsgTie{A.pair_base + p, i};
+                if (slot < A.tie_cap) A.ties[slot] = KsgTie{A.pair_base + p, i, bd[KMAX - 2]};
                 else atomicOr(A.fault, FAULT_TIE_OVERFLOW);
             }
         }

@@ -58,6 +58,15 @@ struct GridArgs {
     float* kdist;
 };
 
+// A frame-mapped row copied out for the cell-grid search:
+// out[c*ld_out + s] = x[c*ld + fmap[s]] for s < m, +inf up to ld_out.
+struct GatherRow {
+    const float* x;
+    const int* fmap;
+    float* out;
+    int ld, m, ld_out;
+};
+
 // Cells per axis for m samples (about ten frames per cell, at most kGridMaxG).
 int grid_cells_per_axis(int m);
 // Node grids (nodes: device array whose x, ld, m, G and buffers are set).
@@ -69,6 +78,9 @@ void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream
 void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st);
 void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a, const int* cnt_b,
                          const float* psi, float* psum, int* nx, int* ny, cudaStream_t st);
+// Copies frame-mapped rows (device array of nrows); a map entry outside
+// [0, ld) sets FAULT_BAD_INDEX in *fault and reads frame 0.
+void grid_launch_gather(const GatherRow* rows, int nrows, int d, int* fault, cudaStream_t st);
 int grid_search_ctas_per_sm(int d, int kmax);
 int grid_count_ctas_per_sm(int d);
 

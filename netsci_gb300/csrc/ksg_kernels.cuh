@@ -294,13 +294,13 @@ __device__ __forceinline__ void eps_and_ties(const KsgCountArgs& A, const KsgIte
 template <int R>
 __device__ __forceinline__ void report_ties(const KsgCountArgs& A, const KsgItem& w,
                                             const int (&qi)[R], const bool (&tie)[R],
-                                            const bool (&mixed)[R]) {
+                                            const bool (&mixed)[R], const float (&wk)[R]) {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         if (tie[r] && mixed[r]) {
             const int slot = atomicAdd(A.tie_count, 1);
             if (slot < A.tie_cap) {
-                A.ties[slot] = KsgTie{w.pair, qi[r]};
+                A.ties[slot] = KsgTie{w.pair, qi[r], wk[r]};
             } else {
                 atomicOr(A.fault, FAULT_TIE_OVERFLOW);
             }
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
                                                  cb, wk, ra, rb, mixed);
             }
         }
-        report_ties<R>(A, w, qi, tie, mixed);
+        report_ties<R>(A, w, qi, tie, mixed, wk);
         write_outputs<KMAX, R>(A, w, P, qi, bd, ea, eb, ca, cb);
     }
 }
@@ -576,7 +576,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel_tma(KsgCountArgs A) {
                 else inflight0 += 1;
             }
         }
-        report_ties<R>(A, w, qi, tie, mixed);
+        report_ties<R>(A, w, qi, tie, mixed, wk);
         write_outputs<KMAX, R>(A, w, P, qi, bd, ea, eb, ca, cb);
     }
 }

@@ -374,11 +374,21 @@ def test_bootstrap_duplicates_and_real_ties(oracle_mod):
     fmap = torch.from_numpy(idx).cuda()
     ab = np.array([[a, b] for a in range(N) for b in range(N) if a != b], np.int32)
     pairs = device.make_pairs(Xd, mm, ab, fmap=fmap, m_samples=m)
-    mi = torch.empty(len(pairs), device="cuda")
-    plan = device.KsgPlan(pairs, k, 3, mi=mi)
-    plan.run()
-    torch.cuda.synchronize()
-    plan.check()
     Xr = X.reshape(N, 3, m)[:, :, idx].reshape(N, 3 * m)
     expect = oracle_mod.pairs(Xr, m, 3, ab, k, gc=False, threads=8)
-    assert np.array_equal(mi.cpu().numpy(), expect)
+    # both searches: exhaustive (copies filtered in its count pass) and cell
+    # grids (resampled rows copied out; copies filtered by the tie kernel)
+    try:
+        for mode, name in ((0, "exhaustive"), (1, "cell-grid")):
+            device.set_ksg_search(mode)
+            mi = torch.empty(len(pairs), device="cuda")
+            plan = device.KsgPlan(pairs, k, 3, mi=mi, graph=True)
+            assert plan.shape["search"] == name
+            for _ in range(2):
+                mi.zero_()
+                plan.run()
+                torch.cuda.synchronize()
+                plan.check()
+                assert np.array_equal(mi.cpu().numpy(), expect), name
+    finally:
+        device.set_ksg_search(-1)

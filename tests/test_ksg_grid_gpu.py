@@ -94,12 +94,30 @@ def test_grid_and_exhaustive_agree_large(grid_search):
     assert np.array_equal(g.cpu().numpy(), e.cpu().numpy())
 
 
-def test_grid_refuses_frame_maps(grid_search):
-    from netsci_gb300 import NsgError, device, synthetic
-    X, _ = synthetic.protein_trajectory(3, 2500, seed=1)
-    Xd, m = device.pack_trajectory(X, 3)
-    fmap = torch.arange(m, dtype=torch.int32, device="cuda")
-    pairs = device.make_pairs(Xd, m, [[0, 1]], fmap=fmap, m_samples=m)
-    with pytest.raises(NsgError) as e:
-        device.KsgPlan(pairs, 6, 3, mi=torch.empty(1, device="cuda"))
-    assert e.value.status == 4
+def test_grid_two_resamples_one_plan(oracle_mod, grid_search):
+    """Pairs of two bootstrap resamples (two frame maps over the same rows)
+    in one cell-grid plan: each resampled row is copied out once, and every
+    MI equals the oracle's on the resampled data."""
+    from netsci_gb300 import device, synthetic
+    N, m, k = 4, 2200, 6
+    X, _ = synthetic.protein_trajectory(N, m, seed=1)
+    Xd, mm = device.pack_trajectory(X, 3)
+    rng = np.random.default_rng(2)
+    ab = synthetic.all_pairs(N)
+    pairs, expect, keep = [], [], []
+    for r in range(2):
+        idx = rng.integers(0, m, size=m).astype(np.int32)
+        fmap = torch.from_numpy(idx).cuda()
+        keep.append(fmap)
+        pairs += device.make_pairs(Xd, mm, ab, fmap=fmap, m_samples=m)
+        Xr = X.reshape(N, 3, m)[:, :, idx].reshape(N, 3 * m)
+        expect += list(oracle_mod.pairs(Xr, m, 3, ab, k, gc=False, threads=8))
+    mi = torch.empty(len(pairs), device="cuda")
+    plan = device.KsgPlan(pairs, k, 3, mi=mi)
+    assert plan.shape["search"] == "cell-grid"
+    # gather, node grids, then pair grids, search, counts, combine, ties, finalize
+    assert plan.launches == 2 + 6
+    plan.run()
+    torch.cuda.synchronize()
+    plan.check()
+    assert np.array_equal(mi.cpu().numpy(), np.asarray(expect, np.float32))
