@@ -7,8 +7,9 @@
 // minimum of single roundings, so the result does not depend on the order k
 // is visited in and matches the CPU restatement bit for bit.
 //
-// Kernel shape: a 128 x 128 output tile per CTA of 256 threads, 8 x 8 outputs
-// per thread, k in slabs of 16 staged in shared memory as interleaved pairs
+// Kernel shape: a 128 x 64 output tile per CTA of 256 threads, 8 x 4 outputs
+// per thread (about 80 registers, three CTAs per SM), k in slabs of 16
+// staged in shared memory as interleaved pairs
 // (k, k+1), so one packed add (add.rn.f32x2) forms two candidate sums and one
 // three-input min folds both into the running minimum: two instructions per
 // two (i, j, k) terms. The work is FADD/FMNMX issue-bound on CUDA cores; a
@@ -28,53 +29,45 @@
 namespace nsg {
 namespace {
 
-constexpr int kTile = 128;
-constexpr int kSlab = 16;  // k values per stage (8 pairs)
+constexpr int kTileI = 128;  // output rows i per CTA
+constexpr int kTileJ = 64;   // output columns j per CTA
+constexpr int kSlab = 16;    // k values per stage (8 pairs)
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-    unsigned long long ra, rb, rr;
-    ra = (static_cast<unsigned long long>(__float_as_uint(a.y)) << 32) | __float_as_uint(a.x);
-    rb = (static_cast<unsigned long long>(__float_as_uint(b.y)) << 32) | __float_as_uint(b.x);
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(rr) : "l"(ra), "l"(rb));
-    return make_float2(__uint_as_float(static_cast<unsigned>(rr & 0xffffffffu)),
-                       __uint_as_float(static_cast<unsigned>(rr >> 32)));
-}
-
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
 hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
                        float* __restrict__ Hn, int n, int* changed, int step) {
     if (step > 0 && changed[step - 1] == 0) return;  // fixed point reached earlier
-    __shared__ __align__(16) float2 Hs[kSlab / 2][kTile];  // (H[k][i], H[k+1][i])
-    __shared__ __align__(16) float2 As[kSlab / 2][kTile];  // (A[j][k], A[j][k+1])
+    __shared__ __align__(16) float2 Hs[kSlab / 2][kTileI];  // (H[k][i], H[k+1][i])
+    __shared__ __align__(16) float2 As[kSlab / 2][kTileJ];  // (A[j][k], A[j][k+1])
     const float inf = __int_as_float(0x7f800000);
     const int tid = threadIdx.x;
-    const int tx = tid & 15;   // i direction
-    const int ty = tid >> 4;   // j direction
-    const int i0 = blockIdx.y * kTile;
-    const int j0 = blockIdx.x * kTile;
+    const int tx = tid & 15;   // i direction: rows tx*4 .. +3 and 64 + tx*4 .. +3
+    const int ty = tid >> 4;   // j direction: columns ty*2, ty*2+1, 32 + ty*2, 32 + ty*2 + 1
+    const int i0 = blockIdx.y * kTileI;
+    const int j0 = blockIdx.x * kTileJ;
 
-    float acc[8][8];
+    float acc[8][4];
 #pragma unroll
     for (int u = 0; u < 8; ++u)
 #pragma unroll
-        for (int v = 0; v < 8; ++v) acc[u][v] = inf;
+        for (int v = 0; v < 4; ++v) acc[u][v] = inf;
 
     for (int k0 = 0; k0 < n; k0 += kSlab) {
         __syncthreads();
         // H slab: rows k0..k0+15, columns i0..i0+127 (coalesced along i)
 #pragma unroll
-        for (int e = 0; e < (kSlab * kTile) / kThreads; ++e) {
+        for (int e = 0; e < (kSlab * kTileI) / kThreads; ++e) {
             const int idx = e * kThreads + tid;
-            const int kk = idx / kTile;
-            const int ii = idx - kk * kTile;
+            const int kk = idx / kTileI;
+            const int ii = idx - kk * kTileI;
             const int k = k0 + kk, i = i0 + ii;
             const float v = (k < n && i < n) ? __ldg(H + (size_t)k * n + i) : inf;
             reinterpret_cast<float*>(&Hs[kk >> 1][ii])[kk & 1] = v;
         }
-        // A slab: rows j0..j0+127, columns k0..k0+15 (coalesced along k)
+        // A slab: rows j0..j0+63, columns k0..k0+15 (coalesced along k)
 #pragma unroll
-        for (int e = 0; e < (kSlab * kTile) / kThreads; ++e) {
+        for (int e = 0; e < (kSlab * kTileJ) / kThreads; ++e) {
             const int idx = e * kThreads + tid;
             const int jj = idx / kSlab;
             const int kk = idx - jj * kSlab;
@@ -85,19 +78,22 @@ hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
         __syncthreads();
 #pragma unroll
         for (int kp = 0; kp < kSlab / 2; ++kp) {
-            float2 h[8], a[8];
+            float2 h[8], a[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 h[u] = Hs[kp][tx * 4 + u];
                 h[u + 4] = Hs[kp][64 + tx * 4 + u];
-                a[u] = As[kp][ty * 4 + u];
-                a[u + 4] = As[kp][64 + ty * 4 + u];
+            }
+#pragma unroll
+            for (int v = 0; v < 2; ++v) {
+                a[v] = As[kp][ty * 2 + v];
+                a[v + 2] = As[kp][32 + ty * 2 + v];
             }
 #pragma unroll
             for (int u = 0; u < 8; ++u)
 #pragma unroll
-                for (int v = 0; v < 8; ++v) {
-                    const float2 s = add2(a[v], h[u]);
+                for (int v = 0; v < 4; ++v) {
+                    const float2 s = nsg_add2(a[v], h[u]);
                     acc[u][v] = nsg_min3(acc[u][v], s.x, s.y);
                 }
         }
@@ -109,8 +105,8 @@ hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
         const int i = i0 + (u < 4 ? tx * 4 + u : 64 + tx * 4 + (u - 4));
         if (i >= n) continue;
 #pragma unroll
-        for (int v = 0; v < 8; ++v) {
-            const int j = j0 + (v < 4 ? ty * 4 + v : 64 + ty * 4 + (v - 4));
+        for (int v = 0; v < 4; ++v) {
+            const int j = j0 + (v < 2 ? ty * 2 + v : 32 + ty * 2 + (v - 2));
             if (j >= n) continue;
             const size_t o = (size_t)i * n + j;
             if (__float_as_int(acc[u][v]) != __float_as_int(__ldg(H + o))) diff = true;
@@ -172,7 +168,7 @@ __global__ void corr_to_adj_kernel(const float* __restrict__ C, float* __restric
 
 void launch_step(const float* A, const float* H, float* Hn, int n, int* changed, int step,
                  cudaStream_t s) {
-    dim3 grid((n + kTile - 1) / kTile, (n + kTile - 1) / kTile);
+    dim3 grid((n + kTileJ - 1) / kTileJ, (n + kTileI - 1) / kTileI);
     hedetniemi_step_kernel<<<grid, kThreads, 0, s>>>(A, H, Hn, n, changed, step);
     NSG_CUDA(cudaGetLastError());
 }

@@ -52,6 +52,19 @@ __device__ __forceinline__ float2 nsg_sub2(float2 a, float2 b) {
     return r;
 }
 
+// Packed add of two float pairs (add.rn.f32x2), assembled the same way.
+__device__ __forceinline__ float2 nsg_add2(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\t"
+        "mov.b64 pa, {%2, %3};\n\t"
+        "mov.b64 pb, {%4, %5};\n\t"
+        "add.rn.f32x2 pr, pa, pb;\n\t"
+        "mov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
 // Bounded mbarrier wait (phase parity). Returns false when the iteration
 // limit runs out; callers record FAULT_WAIT_TIMEOUT and leave.
 __device__ __forceinline__ bool nsg_mbar_wait(uint32_t bar_smem, uint32_t parity,
