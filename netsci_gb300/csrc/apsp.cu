@@ -33,6 +33,8 @@ constexpr int kTileI = 128;  // output rows i per CTA
 constexpr int kTileJ = 64;   // output columns j per CTA
 constexpr int kSlab = 16;    // k values per stage (8 pairs)
 constexpr int kThreads = 256;
+constexpr int kHLoads = (kSlab * kTileI) / kThreads;  // elements per thread per slab
+constexpr int kALoads = (kSlab * kTileJ) / kThreads;
 
 __global__ void __launch_bounds__(kThreads, 2)
 hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
@@ -42,8 +44,11 @@ hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
     __shared__ __align__(16) float2 As[kSlab / 2][kTileJ];  // (A[j][k], A[j][k+1])
     const float inf = __int_as_float(0x7f800000);
     const int tid = threadIdx.x;
-    const int tx = tid & 15;   // i direction: rows tx*4 .. +3 and 64 + tx*4 .. +3
-    const int ty = tid >> 4;   // j direction: columns ty*2, ty*2+1, 32 + ty*2, 32 + ty*2 + 1
+    // Rows i = i0 + 32w + 2tx + {0,1} for w = 0..3: the lanes of a warp read
+    // consecutive 16-byte pairs of Hs (no bank replays). Columns
+    // j = j0 + 32w + 2ty + {0,1} for w = 0..1: two addresses per warp.
+    const int tx = tid & 15;
+    const int ty = tid >> 4;
     const int i0 = blockIdx.y * kTileI;
     const int j0 = blockIdx.x * kTileJ;
 
@@ -53,41 +58,56 @@ hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = inf;
 
-    for (int k0 = 0; k0 < n; k0 += kSlab) {
-        __syncthreads();
-        // H slab: rows k0..k0+15, columns i0..i0+127 (coalesced along i)
+    // the next slab is loaded into registers while the current one is used
+    float hv[kHLoads], av[kALoads];
+    auto load_slab = [&](int k0) {
 #pragma unroll
-        for (int e = 0; e < (kSlab * kTileI) / kThreads; ++e) {
+        for (int e = 0; e < kHLoads; ++e) {
             const int idx = e * kThreads + tid;
             const int kk = idx / kTileI;
             const int ii = idx - kk * kTileI;
             const int k = k0 + kk, i = i0 + ii;
-            const float v = (k < n && i < n) ? __ldg(H + (size_t)k * n + i) : inf;
-            reinterpret_cast<float*>(&Hs[kk >> 1][ii])[kk & 1] = v;
+            hv[e] = (k < n && i < n) ? __ldg(H + (size_t)k * n + i) : inf;
         }
-        // A slab: rows j0..j0+63, columns k0..k0+15 (coalesced along k)
 #pragma unroll
-        for (int e = 0; e < (kSlab * kTileJ) / kThreads; ++e) {
+        for (int e = 0; e < kALoads; ++e) {
             const int idx = e * kThreads + tid;
             const int jj = idx / kSlab;
             const int kk = idx - jj * kSlab;
             const int k = k0 + kk, j = j0 + jj;
-            const float v = (k < n && j < n) ? __ldg(A + (size_t)j * n + k) : inf;
-            reinterpret_cast<float*>(&As[kk >> 1][jj])[kk & 1] = v;
+            av[e] = (k < n && j < n) ? __ldg(A + (size_t)j * n + k) : inf;
+        }
+    };
+    load_slab(0);
+    for (int k0 = 0; k0 < n; k0 += kSlab) {
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < kHLoads; ++e) {
+            const int idx = e * kThreads + tid;
+            const int kk = idx / kTileI;
+            reinterpret_cast<float*>(&Hs[kk >> 1][idx - kk * kTileI])[kk & 1] = hv[e];
+        }
+#pragma unroll
+        for (int e = 0; e < kALoads; ++e) {
+            const int idx = e * kThreads + tid;
+            const int jj = idx / kSlab;
+            const int kk = idx - jj * kSlab;
+            reinterpret_cast<float*>(&As[kk >> 1][jj])[kk & 1] = av[e];
         }
         __syncthreads();
+        if (k0 + kSlab < n) load_slab(k0 + kSlab);
 #pragma unroll
         for (int kp = 0; kp < kSlab / 2; ++kp) {
             float2 h[8], a[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                h[u] = Hs[kp][tx * 4 + u];
-                h[u + 4] = Hs[kp][64 + tx * 4 + u];
+            for (int w = 0; w < 4; ++w) {
+                h[2 * w] = Hs[kp][32 * w + 2 * tx];
+                h[2 * w + 1] = Hs[kp][32 * w + 2 * tx + 1];
             }
 #pragma unroll
-            for (int v = 0; v < 2; ++v) {
-                a[v] = As[kp][ty * 2 + v];
-                a[v + 2] = As[kp][32 + ty * 2 + v];
+            for (int w = 0; w < 2; ++w) {
+                a[2 * w] = As[kp][32 * w + 2 * ty];
+                a[2 * w + 1] = As[kp][32 * w + 2 * ty + 1];
             }
 #pragma unroll
             for (int u = 0; u < 8; ++u)
@@ -102,11 +122,11 @@ hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
     bool diff = false;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-        const int i = i0 + (u < 4 ? tx * 4 + u : 64 + tx * 4 + (u - 4));
+        const int i = i0 + 32 * (u >> 1) + 2 * tx + (u & 1);
         if (i >= n) continue;
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            const int j = j0 + (v < 2 ? ty * 2 + v : 32 + ty * 2 + (v - 2));
+            const int j = j0 + 32 * (v >> 1) + 2 * ty + (v & 1);
             if (j >= n) continue;
             const size_t o = (size_t)i * n + j;
             if (__float_as_int(acc[u][v]) != __float_as_int(__ldg(H + o))) diff = true;
