@@ -468,9 +468,16 @@ def main():
             t0 = time.perf_counter()
             H, steps = device.apsp_lengths(A, n_g)
             torch.cuda.synchronize()
-            apsp[f"{name}_ms"] = 1000 * (time.perf_counter() - t0)
+            dt_a = time.perf_counter() - t0
+            apsp[f"{name}_ms"] = 1000 * dt_a
             apsp[f"{name}_steps"] = steps
+            # min-plus terms (one add and one min per (i, j, k)) per second,
+            # against one term per lane per cycle (packed add + 3-input min:
+            # two instructions per two terms)
+            apsp[f"{name}_terms_per_s"] = n_g ** 3 * steps / dt_a
         apsp["n"] = n_g
+        apsp["terms_peak_per_s"] = props.multi_processor_count * 128 * sm_max * 1e6
+        apsp["frac"] = apsp["rgg_int_terms_per_s"] / apsp["terms_peak_per_s"]
 
     # ---- other configurations (rank 0) ----------------------------------------------
     extra = {}
