@@ -58,16 +58,16 @@ hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = inf;
 
-    // the next slab is loaded into registers while the current one is used
-    float hv[kHLoads], av[kALoads];
-    auto load_slab = [&](int k0) {
+    for (int k0 = 0; k0 < n; k0 += kSlab) {
+        __syncthreads();
 #pragma unroll
         for (int e = 0; e < kHLoads; ++e) {
             const int idx = e * kThreads + tid;
             const int kk = idx / kTileI;
             const int ii = idx - kk * kTileI;
             const int k = k0 + kk, i = i0 + ii;
-            hv[e] = (k < n && i < n) ? __ldg(H + (size_t)k * n + i) : inf;
+            reinterpret_cast<float*>(&Hs[kk >> 1][ii])[kk & 1] =
+                (k < n && i < n) ? __ldg(H + (size_t)k * n + i) : inf;
         }
 #pragma unroll
         for (int e = 0; e < kALoads; ++e) {
@@ -75,27 +75,10 @@ hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
             const int jj = idx / kSlab;
             const int kk = idx - jj * kSlab;
             const int k = k0 + kk, j = j0 + jj;
-            av[e] = (k < n && j < n) ? __ldg(A + (size_t)j * n + k) : inf;
-        }
-    };
-    load_slab(0);
-    for (int k0 = 0; k0 < n; k0 += kSlab) {
-        __syncthreads();
-#pragma unroll
-        for (int e = 0; e < kHLoads; ++e) {
-            const int idx = e * kThreads + tid;
-            const int kk = idx / kTileI;
-            reinterpret_cast<float*>(&Hs[kk >> 1][idx - kk * kTileI])[kk & 1] = hv[e];
-        }
-#pragma unroll
-        for (int e = 0; e < kALoads; ++e) {
-            const int idx = e * kThreads + tid;
-            const int jj = idx / kSlab;
-            const int kk = idx - jj * kSlab;
-            reinterpret_cast<float*>(&As[kk >> 1][jj])[kk & 1] = av[e];
+            reinterpret_cast<float*>(&As[kk >> 1][jj])[kk & 1] =
+                (k < n && j < n) ? __ldg(A + (size_t)j * n + k) : inf;
         }
         __syncthreads();
-        if (k0 + kSlab < n) load_slab(k0 + kSlab);
 #pragma unroll
         for (int kp = 0; kp < kSlab / 2; ++kp) {
             float2 h[8], a[4];
