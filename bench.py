@@ -17,6 +17,9 @@ Lines reported (one JSON line from rank 0):
             and device->host read of the results inside every step.
   plain_per_call  pairs/s of one netcalc.generalizedCorrelationGpu call per
             pair (the reference's call structure) on a small sample.
+  exhaustive_search  the same steps with the exhaustive neighbour search (every
+            frame against every query): pairs/s, its count kernel's fraction of
+            the issue peak, and whether its GC equals the cell-grid run's.
   apsp      Hedetniemi shortest-path ms on N = 2000 random geometric graphs
             (mean degree 12), integer weights U[1,100] and float weights.
   roofline  the neighbour-search kernels against the CUDA-core issue peak
@@ -404,6 +407,37 @@ def main():
     if clocks.get("sm_mhz"):
         frac_at_clock = achieved / (props.multi_processor_count * 128 * clocks["sm_mhz"] * 1e6 / 1e9)
 
+    # ---- the exhaustive search on the same workload, for comparison ----------------
+    exhaustive = None
+    if not args.quick:
+        device.set_ksg_search(0)
+        try:
+            ex_plans = []
+            for s_ in range(3):
+                g_ = torch.empty(B, device="cuda")
+                ex_plans.append((device.KsgPlan(device.make_pairs(Xd, mm, slice_for(s_)), K_NN, DIM,
+                                                gc=g_, graph=True, timing=True), g_))
+            ex_plans[0][0].run()
+            torch.cuda.synchronize()
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for pl, _ in ex_plans[1:]:
+                pl.run()
+            e1.record()
+            torch.cuda.synchronize()
+            ex_ms = max_over_ranks(e0.elapsed_time(e1)) / (len(ex_plans) - 1)
+            ex_count = statistics.mean(pl.count_ms() for pl, _ in ex_plans[1:]) / 1000.0
+            same = all(np.array_equal(g_.cpu().numpy(), outs[s_].cpu().numpy())
+                       for s_, (_, g_) in enumerate(ex_plans[1:], start=1) if s_ < S)
+            exhaustive = {"value": world * B / (ex_ms / 1000.0), "unit": "pairs/s", "ms_per_step": ex_ms,
+                          "steps": len(ex_plans) - 1, "count_kernel_frac_of_peak": ops_launch / ex_count / 1e9 / peak_gops,
+                          "same_gc_as_cell_grid": bool(same)}
+            for pl, _ in ex_plans:
+                pl.close()
+        finally:
+            device.set_ksg_search(-1)
+
     # ---- e2e through the drop-in CuArray API -------------------------------------
     e2e = None
     if not args.no_e2e:
@@ -510,7 +544,7 @@ def main():
                        "parallelism": f"pairs sharded over {world} GPU(s), no collective",
                        "l2": "inputs larger than L2 (X resident, 241 MB > 129 MB L2)",
                        "tile": plans[0].shape},
-            "e2e": e2e, "plain_per_call": plain, "apsp": apsp,
+            "e2e": e2e, "plain_per_call": plain, "exhaustive_search": exhaustive, "apsp": apsp,
             "gpu_launches": launches,
             "roofline": {"bound": "cuda_core_issue", "achieved": achieved,
                          "peak": peak_gops, "unit": "Gop/s", "frac": achieved / peak_gops,
