@@ -506,6 +506,9 @@ struct KsgPlan::GridState {
     DeviceBuffer gps, pair_arena;         // GridPair per plan pair; pair grids of one batch
     DeviceBuffer wprefix;                 // per batch: npairs+1 prefix of ceil(m/32)
     std::vector<long long> wprefix_off;   // offset of each batch's prefix
+    DeviceBuffer groups, gprefix;         // count groups and their item prefix, per batch
+    std::vector<long long> group_off, gprefix_off;
+    std::vector<int> ngroups;
     DeviceBuffer eps_a, eps_b, cnt_a, cnt_b;
     DeviceBuffer evals;                   // 2 counters per run (search, counts)
     int nnodes = 0;
@@ -607,6 +610,31 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
         gp.perm = reinterpret_cast<int*>(pbase + reinterpret_cast<uintptr_t>(gp.perm));
         gp.sx = reinterpret_cast<float*>(pbase + reinterpret_cast<uintptr_t>(gp.sx));
     }
+    // count groups: pairs of a batch that count the same node's variable
+    {
+        std::vector<CountGroup> groups;
+        std::vector<int> gpre;
+        for (const Batch& b : batches_) {
+            g->group_off.push_back(static_cast<long long>(groups.size()));
+            g->gprefix_off.push_back(static_cast<long long>(gpre.size()));
+            const size_t first = groups.size();
+            append_count_groups(gps.data() + b.pair0, b.npairs, groups);
+            int acc = 0;
+            for (size_t gi = first; gi < groups.size(); ++gi) {
+                gpre.push_back(acc);
+                acc += (nodes[groups[gi].node].m + 31) / 32;
+            }
+            gpre.push_back(acc);
+            g->ngroups.push_back(static_cast<int>(groups.size() - first));
+        }
+        g->groups.reset(std::max<size_t>(1, groups.size()) * sizeof(CountGroup));
+        if (!groups.empty()) {
+            NSG_CUDA(cudaMemcpy(g->groups.get(), groups.data(), groups.size() * sizeof(CountGroup),
+                                cudaMemcpyHostToDevice));
+        }
+        g->gprefix.reset(gpre.size() * sizeof(int));
+        NSG_CUDA(cudaMemcpy(g->gprefix.get(), gpre.data(), gpre.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
     g->gps.reset(gps.size() * sizeof(GridPair));
     NSG_CUDA(cudaMemcpy(g->gps.get(), gps.data(), gps.size() * sizeof(GridPair), cudaMemcpyHostToDevice));
     g->wprefix.reset(wpre.size() * sizeof(int));
@@ -640,6 +668,9 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         a.gp = bg;
         a.nodes = g.nodes.as<GridNode>();
         a.wprefix = g.wprefix.as<int>() + g.wprefix_off[bi];
+        a.groups = g.groups.as<CountGroup>() + g.group_off[bi];
+        a.gprefix = g.gprefix.as<int>() + g.gprefix_off[bi];
+        a.ngroups = g.ngroups[bi];
         a.npairs = b.npairs;
         a.pair_base = b.pair0;
         a.k = k_;

@@ -2,6 +2,8 @@
 // pass-1 / count kernels and their launchers (ksg_grid.cuh has the search).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "errors.h"
 #include "ksg_grid.cuh"
 #include "ksg_grid.h"
@@ -229,6 +231,27 @@ void launch_pass1(const GridArgs& a, int kmax, int grid, cudaStream_t st) {
 }
 
 }  // namespace
+
+void append_count_groups(const GridPair* gps, int npairs, std::vector<CountGroup>& out) {
+    for (int side = 0; side < 2; ++side) {
+        // pairs by node, in first-appearance order of the nodes
+        std::vector<std::pair<int, int>> keyed(npairs);
+        for (int p = 0; p < npairs; ++p) keyed[p] = {side ? gps[p].b : gps[p].a, p};
+        std::stable_sort(keyed.begin(), keyed.end(),
+                         [](const std::pair<int, int>& x, const std::pair<int, int>& y) { return x.first < y.first; });
+        for (size_t s = 0; s < keyed.size();) {
+            CountGroup g{};
+            g.node = keyed[s].first;
+            g.side = side;
+            while (s < keyed.size() && keyed[s].first == g.node && g.npairs < kCountGroup) {
+                g.pairs[g.npairs++] = keyed[s].second;
+                ++s;
+            }
+            for (int q = g.npairs; q < kCountGroup; ++q) g.pairs[q] = g.pairs[0];
+            out.push_back(g);
+        }
+    }
+}
 
 int grid_cells_per_axis(int m) {
     int g = 1;

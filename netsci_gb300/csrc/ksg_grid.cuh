@@ -161,10 +161,12 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
     }
 }
 
+// Counts over a staged chunk for up to kCountGroup pairs at once: one
+// distance per frame, compared with each pair's eps (unused slots hold -inf).
 template <int D>
-__device__ __forceinline__ int count_chunk(const float* tile, int n, const float (&q)[D], float e) {
+__device__ __forceinline__ void count_chunk(const float* tile, int n, const float (&q)[D],
+                                            const float (&e)[kCountGroup], int (&cnt)[kCountGroup]) {
     const int ngroups = (n + 3) >> 2;
-    int cnt = 0;
     for (int g = 0; g < ngroups; ++g) {
         float4 gq[D];
 #pragma unroll
@@ -172,9 +174,10 @@ __device__ __forceinline__ int count_chunk(const float* tile, int n, const float
         float dq[4];
         ksgk::Marg<D, 1>::four(q, gq, dq);
 #pragma unroll
-        for (int f = 0; f < 4; ++f) cnt += dq[f] <= e ? 1 : 0;
+        for (int f = 0; f < 4; ++f)
+#pragma unroll
+            for (int p = 0; p < kCountGroup; ++p) cnt[p] += dq[f] <= e[p] ? 1 : 0;
     }
-    return cnt;
 }
 
 }  // namespace gridk
@@ -338,8 +341,10 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
 }
 
 // ---- pass 2: marginal counts on a node grid -------------------------------------
-// Work items 0 .. total-1 count variable a of each pair, total .. 2*total-1
-// variable b.
+// A work item is a count group (up to kCountGroup pairs that count the same
+// node's variable) and a block of 32 queries consecutive in that node's grid;
+// the warp visits the union of the queries' boxes for the largest of the
+// pairs' eps and counts every pair from one distance per frame.
 template <int D>
 __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArgs A) {
     using namespace gridk;
@@ -347,21 +352,19 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     float* tile = s_tile[wid];
-    const int total = __ldg(A.wprefix + A.npairs);
+    const int total = __ldg(A.gprefix + A.ngroups);
     for (;;) {
         int t = 0;
         if (lane == 0) t = atomicAdd(A.counter, 1);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= 2 * total) return;
-        const bool side_b = t >= total;
-        int p, blk;
-        item_of(A.wprefix, A.npairs, side_b ? t - total : t, p, blk);
-        const KsgPairDesc P = A.pairs[p];
-        const GridPair gp = A.gp[p];
-        const GridNode nd = A.nodes[side_b ? gp.b : gp.a];
-        const float* eps = side_b ? A.eps_b : A.eps_a;
-        int* out = side_b ? A.cnt_b : A.cnt_a;
-        const int m = P.m, G = nd.G;
+        if (t >= total) return;
+        int gi, blk;
+        item_of(A.gprefix, A.ngroups, t, gi, blk);
+        const CountGroup grp = A.groups[gi];
+        const GridNode nd = A.nodes[grp.node];
+        const float* eps = grp.side ? A.eps_b : A.eps_a;
+        int* out = grp.side ? A.cnt_b : A.cnt_a;
+        const int m = nd.m, G = nd.G;
         const long long st = m;
         const int r = blk * 32 + lane;
         const bool valid = r < m;
@@ -369,19 +372,29 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
         float q[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) q[c] = valid ? __ldg(nd.sx + c * st + r) : 0.f;
-        const float e = valid ? __ldg(eps + P.scratch + i) : -inf_f();
+        float e[kCountGroup];
+        long long o[kCountGroup];
+        float emax = -inf_f();
+#pragma unroll
+        for (int p = 0; p < kCountGroup; ++p) {
+            o[p] = p < grp.npairs ? A.pairs[grp.pairs[p]].scratch + i : 0;
+            e[p] = (valid && p < grp.npairs) ? __ldg(eps + o[p]) : -inf_f();
+            emax = fmaxf(emax, e[p]);
+        }
         const float q1 = q[nd.c1];
         const float q2 = nd.c2 >= 0 ? q[nd.c2] : 0.f;
         int rlo = G, rhi = -1, clo = G, chi = -1;
         if (valid) {
-            bin_range(nd.e1, G, q1, e, rlo, rhi);
-            bin_range(nd.e2, G, q2, e, clo, chi);
+            bin_range(nd.e1, G, q1, emax, rlo, rhi);
+            bin_range(nd.e2, G, q2, emax, clo, chi);
         }
         rlo = warp_min(rlo);
         rhi = warp_max(rhi);
         clo = warp_min(clo);
         chi = warp_max(chi);
-        int cnt = 0;
+        int cnt[kCountGroup];
+#pragma unroll
+        for (int p = 0; p < kCountGroup; ++p) cnt[p] = 0;
         long long scanned = 0;
         for (int cx = rlo; cx <= rhi && clo <= chi; ++cx) {
             const int lo = __ldg(nd.start + cx * G + clo);
@@ -392,12 +405,17 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
                 __syncwarp();
                 stage<D, false>(tile, nullptr, nd.sx, st, nullptr, base, n, lane);
                 __syncwarp();
-                cnt += count_chunk<D>(tile, n, q, e);
+                count_chunk<D>(tile, n, q, e, cnt);
             }
         }
-        if (valid) out[P.scratch + i] = cnt;
+        if (valid) {
+#pragma unroll
+            for (int p = 0; p < kCountGroup; ++p)
+                if (p < grp.npairs) out[o[p]] = cnt[p];
+        }
         if (A.evals && lane == 0) {
-            atomicAdd(A.evals + 1, static_cast<unsigned long long>(scanned) * min(32, m - blk * 32));
+            atomicAdd(A.evals + 1,
+                      static_cast<unsigned long long>(scanned) * min(32, m - blk * 32) * grp.npairs);
         }
     }
 }

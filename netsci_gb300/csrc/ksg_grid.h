@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "ksg.cuh"
 
 namespace nsg {
@@ -33,11 +35,24 @@ struct GridPair {
     float* sx;             // [2d][m] coordinates of a then b in that order
 };
 
+// Pairs of a batch that count the same variable (node grid): their counts
+// share every distance evaluation.
+constexpr int kCountGroup = 4;
+struct CountGroup {
+    int node;                      // node grid
+    int side;                      // 0: variable a of the pairs, 1: variable b
+    int npairs;                    // 1..kCountGroup
+    int pairs[kCountGroup];        // batch-relative pair indices
+};
+
 struct GridArgs {
     const KsgPairDesc* pairs;   // batch pairs (scratch offsets, m, out)
     const GridPair* gp;         // same indexing as pairs
     const GridNode* nodes;
-    const int* wprefix;         // [npairs+1] prefix of ceil(m/32) over the batch
+    const int* wprefix;         // [npairs+1] prefix of ceil(m/32) over the batch (search items)
+    const CountGroup* groups;   // count groups of the batch
+    const int* gprefix;         // [ngroups+1] prefix of ceil(m/32) over the groups (count items)
+    int ngroups;
     int npairs;
     int pair_base;              // index of pairs[0] in the plan's pair array (tie entries)
     int k;
@@ -66,6 +81,11 @@ struct GatherRow {
     float* out;
     int ld, m, ld_out;
 };
+
+// Appends the count groups of npairs pairs (descriptors with node indices a,
+// b; pair indices relative to gps): for each side, the pairs that count the
+// same node, in order, kCountGroup at a time.
+void append_count_groups(const GridPair* gps, int npairs, std::vector<CountGroup>& out);
 
 // Cells per axis for m samples (about ten frames per cell, at most kGridMaxG).
 int grid_cells_per_axis(int m);

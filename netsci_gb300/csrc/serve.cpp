@@ -142,6 +142,8 @@ Server::Server(const ServerConfig& cfg) : cfg_(cfg) {
     d_gnodes_.reset(sizeof(GridNode) * kNodeSlots);
     d_gpairs_.reset(sizeof(GridPair) * kGridTickPairs);
     d_wpre_.reset(sizeof(int) * (kGridTickPairs + 1));
+    d_groups_.reset(sizeof(CountGroup) * 2 * kGridTickPairs);
+    d_gpre_.reset(sizeof(int) * (2 * kGridTickPairs + 1));
     NSG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h_gpairs_), sizeof(GridPair) * kGridTickPairs));
     NSG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h_wpre_), sizeof(int) * (kGridTickPairs + 1)));
     for (int i = kMiSlotPairs - 1; i >= 0; --i) free_mi_slots_.push_back(kNodeSlots - 2 * (i + 1));
@@ -460,6 +462,16 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     NSG_CUDA(cudaMemcpyAsync(d_pairs_.get(), h_pairs_, sizeof(KsgPairDesc) * np, cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemcpyAsync(d_gpairs_.get(), h_gpairs_, sizeof(GridPair) * np, cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemcpyAsync(d_wpre_.get(), h_wpre_, sizeof(int) * (np + 1), cudaMemcpyHostToDevice, s));
+    // count groups: pairs of the tick that count the same node's variable
+    std::vector<CountGroup> groups;
+    append_count_groups(h_gpairs_, static_cast<int>(np), groups);
+    std::vector<int> gpre(groups.size() + 1, 0);
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        gpre[gi + 1] = gpre[gi] + (h_pairs_[groups[gi].pairs[0]].m + 31) / 32;
+    }
+    NSG_CUDA(cudaMemcpyAsync(d_groups_.get(), groups.data(), sizeof(CountGroup) * groups.size(),
+                             cudaMemcpyHostToDevice, s));
+    NSG_CUDA(cudaMemcpyAsync(d_gpre_.get(), gpre.data(), sizeof(int) * gpre.size(), cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemsetAsync(d_counters_.get(), 0, sizeof(int) * 4, s));
     int* ctr = d_counters_.as<int>();
     KsgPairDesc* dp = d_pairs_.as<KsgPairDesc>();
@@ -469,6 +481,9 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     a.gp = d_gpairs_.as<GridPair>();
     a.nodes = d_gnodes_.as<GridNode>();
     a.wprefix = d_wpre_.as<int>();
+    a.groups = d_groups_.as<CountGroup>();
+    a.gprefix = d_gpre_.as<int>();
+    a.ngroups = static_cast<int>(groups.size());
     a.npairs = static_cast<int>(np);
     a.pair_base = 0;
     a.k = k;

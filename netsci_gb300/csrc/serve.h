@@ -103,6 +103,7 @@ private:
     // the bottom, pairs of slots for MI jobs from a free list at the top),
     // and per-tick pair grids and scratch, grown on demand
     DeviceBuffer d_gnodes_, d_gpairs_, d_wpre_, d_garena_, d_eps_a_, d_eps_b_, d_cnt_a_, d_cnt_b_;
+    DeviceBuffer d_groups_, d_gpre_;
     GridPair* h_gpairs_ = nullptr;
     int* h_wpre_ = nullptr;
     int next_node_slot_ = 0;
