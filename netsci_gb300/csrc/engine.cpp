@@ -417,10 +417,8 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const 
             std::max<long long>(65536, bootstrap_ ? batch_samples : batch_samples / 4), 1LL << 30));
         ties_.reset(static_cast<size_t>(tie_cap_) * sizeof(KsgTie));
         tie_stride_ = maxm;
-        if (!ksg_tie_rows_in_smem(tie_stride_)) {
-            tie_dz_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(float));
-            tie_idx_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(int));
-        }
+        tie_dz_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(float));
+        tie_idx_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(int));
         fault_.reset(sizeof(int));
         NSG_CUDA(cudaMemset(fault_.get(), 0, sizeof(int)));
         psi_ = device_psi(maxm);

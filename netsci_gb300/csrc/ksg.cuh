@@ -114,9 +114,6 @@ void ksg_launch_counts(const KsgCountArgs& a, int d, int kmax, const KsgShape& s
 void ksg_launch_final(const KsgFinalArgs& a, cudaStream_t st);
 // Warps the tie kernel runs with (scratch rows needed).
 int ksg_tie_warps();
-// True when ksg_launch_ties keeps the rows of `stride` samples in shared
-// memory (the caller's dz / idx scratch is then unused).
-bool ksg_tie_rows_in_smem(long long stride);
 void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st);
 void ksg_launch_ties_ctas(const KsgTieArgs& a, int d, int ctas, cudaStream_t st);
 // One pair with all scratch in the library's static device area

@@ -18,8 +18,6 @@
 // Runs between the count kernel and the finalize kernel, with a fixed grid
 // that walks the tie list through an atomic counter (an empty list costs one
 // launch that returns at once).
-#include <algorithm>
-
 #include "common.cuh"
 #include "engine.h"
 #include "ksg.cuh"
@@ -33,7 +31,6 @@ constexpr int kWarpsPerCta = 8;
 constexpr int kCtasPerSm = 2;
 constexpr int kStack = 64;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kTieSmemBytes = 200 << 10;  // rows up to 25600 samples in shared memory
 
 __device__ __forceinline__ int tie_frame(const int* __restrict__ fmap, int s, int ld, int* fault) {
     if (!fmap) return s;
@@ -54,16 +51,12 @@ __device__ __forceinline__ float tie_marginal(const float (&q)[D], const float* 
     return v;
 }
 
-// SMEM: one warp per CTA with its distance and index rows in shared memory
-// (the serial sort replay reads them at shared-memory latency); otherwise
-// kWarpsPerCta warps per CTA with rows in the caller's device scratch.
-template <int D, bool SMEM>
+template <int D>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) ksg_tie_kernel(KsgTieArgs A) {
-    extern __shared__ __align__(16) float s_rows[];
     const int lane = threadIdx.x & 31;
     const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    float* dz = SMEM ? s_rows : A.dz + warp * A.stride;
-    int* idx = SMEM ? reinterpret_cast<int*>(s_rows + A.stride) : A.idx + warp * A.stride;
+    float* dz = A.dz + warp * A.stride;
+    int* idx = A.idx + warp * A.stride;
     const int total = min(*A.tie_count, A.tie_cap);
     for (;;) {
         int e = 0;
@@ -186,45 +179,13 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) ksg_tie_kernel(KsgTieArgs A
 
 int ksg_tie_warps() { return sm_count() * kCtasPerSm * kWarpsPerCta; }
 
-bool ksg_tie_rows_in_smem(long long stride) {
-    return stride * 8 <= kTieSmemBytes;
-}
-
-namespace {
-template <int D>
-void launch_smem_ties(const KsgTieArgs& a, cudaStream_t st) {
-    static bool configured[16] = {false};
-    int dev = 0;
-    NSG_CUDA(cudaGetDevice(&dev));
-    if (!configured[dev & 15]) {
-        NSG_CUDA(cudaFuncSetAttribute(ksg_tie_kernel<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      kTieSmemBytes));
-        configured[dev & 15] = true;
-    }
-    const size_t bytes = static_cast<size_t>(a.stride) * 8;
-    // as many one-warp CTAs per SM as the rows allow
-    const int per_sm = static_cast<int>(std::max<size_t>(1, std::min<size_t>(16, (228u << 10) / (bytes + 1024))));
-    ksg_tie_kernel<D, true><<<sm_count() * per_sm, 32, bytes, st>>>(a);
-}
-}  // namespace
-
 void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st) {
-    if (ksg_tie_rows_in_smem(a.stride)) {
-        switch (d) {
-            case 1: launch_smem_ties<1>(a, st); break;
-            case 2: launch_smem_ties<2>(a, st); break;
-            case 3: launch_smem_ties<3>(a, st); break;
-            default: fail(NSG_ERR_INVALID, "d must be 1, 2 or 3");
-        }
-        NSG_CUDA(cudaGetLastError());
-        return;
-    }
     const int grid = sm_count() * kCtasPerSm;
     const int threads = kWarpsPerCta * 32;
     switch (d) {
-        case 1: ksg_tie_kernel<1, false><<<grid, threads, 0, st>>>(a); break;
-        case 2: ksg_tie_kernel<2, false><<<grid, threads, 0, st>>>(a); break;
-        case 3: ksg_tie_kernel<3, false><<<grid, threads, 0, st>>>(a); break;
+        case 1: ksg_tie_kernel<1><<<grid, threads, 0, st>>>(a); break;
+        case 2: ksg_tie_kernel<2><<<grid, threads, 0, st>>>(a); break;
+        case 3: ksg_tie_kernel<3><<<grid, threads, 0, st>>>(a); break;
         default: fail(NSG_ERR_INVALID, "d must be 1, 2 or 3");
     }
     NSG_CUDA(cudaGetLastError());
@@ -235,9 +196,9 @@ void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st) {
 void ksg_launch_ties_ctas(const KsgTieArgs& a, int d, int ctas, cudaStream_t st) {
     const int threads = kWarpsPerCta * 32;
     switch (d) {
-        case 1: ksg_tie_kernel<1, false><<<ctas, threads, 0, st>>>(a); break;
-        case 2: ksg_tie_kernel<2, false><<<ctas, threads, 0, st>>>(a); break;
-        case 3: ksg_tie_kernel<3, false><<<ctas, threads, 0, st>>>(a); break;
+        case 1: ksg_tie_kernel<1><<<ctas, threads, 0, st>>>(a); break;
+        case 2: ksg_tie_kernel<2><<<ctas, threads, 0, st>>>(a); break;
+        case 3: ksg_tie_kernel<3><<<ctas, threads, 0, st>>>(a); break;
         default: fail(NSG_ERR_INVALID, "d must be 1, 2 or 3");
     }
     NSG_CUDA(cudaGetLastError());
