@@ -51,8 +51,139 @@ __device__ __forceinline__ float tie_marginal(const float (&q)[D], const float* 
     return v;
 }
 
+// sort_prefix_like_reference (sort_prefix.h) run by a whole warp: the same
+// segments, pivots and swaps, with each unguarded partition found 32
+// positions at a time. The partition of [first+1, last) around pk swaps the
+// t-th element from the left that is not below pk (a left stopper) with the
+// t-th element from the right that is not above pk (a right stopper, the
+// scan may reach the pivot itself at `first`) while the former lies left of
+// the latter; the elements between them are untouched until then, so the
+// stoppers can be read from the array as it was. The cut is the first left
+// stopper past the last swap, or that swap's right position if it comes
+// first. Lane 0 holds the segment stack and does the swaps; all lanes load
+// and vote. Same result as the serial routine, element for element.
+__device__ bool sort_prefix_warp(const float* key, int* idx, int n, int T, SortSegment* stack,
+                                 int cap, int lane) {
+    if (n <= 1) return true;
+    constexpr int kThreshold = 16;
+    int top = 0;
+    if (lane == 0) stack[0] = {0, n, 2 * floor_log2(n)};
+    top = 1;
+    int prefix_end = 0;
+    while (top > 0) {
+        --top;
+        SortSegment sg{};
+        if (lane == 0) sg = stack[top];
+        int first = __shfl_sync(kFull, sg.first, 0);
+        int last = __shfl_sync(kFull, sg.last, 0);
+        int depth = __shfl_sync(kFull, sg.depth, 0);
+        while (last - first > kThreshold) {
+            if (depth == 0) return false;
+            --depth;
+            // median of three moved to `first` (lane 0)
+            if (lane == 0) {
+                const int a = first + 1, b = first + (last - first) / 2, c = last - 1;
+                const float ka = key[idx[a]], kb = key[idx[b]], kc = key[idx[c]];
+                int pick;
+                if (ka < kb) {
+                    if (kb < kc) pick = b;
+                    else if (ka < kc) pick = c;
+                    else pick = a;
+                } else if (ka < kc) {
+                    pick = a;
+                } else if (kb < kc) {
+                    pick = c;
+                } else {
+                    pick = b;
+                }
+                const int t = idx[first];
+                idx[first] = idx[pick];
+                idx[pick] = t;
+            }
+            __syncwarp();
+            const float pk = key[idx[first]];
+            // left stoppers from first+1 up, right stoppers from last-1 down
+            int lbase = first + 1, rbase = last - 1;  // next chunk starts
+            int lchunk = 0, rchunk = 0;               // current chunk starts
+            unsigned lmask = 0, rmask = 0;
+            bool lend = false, rend = false;
+            int prev_r = -1;                          // right position of the last swap
+            int cut;
+            for (;;) {
+                while (lmask == 0 && !lend) {
+                    if (lbase >= last) {
+                        lend = true;
+                        break;
+                    }
+                    const int p = lbase + lane;
+                    const bool st = p < last && !(key[idx[p]] < pk);
+                    lmask = __ballot_sync(kFull, st);
+                    lchunk = lbase;
+                    lbase += 32;
+                }
+                while (rmask == 0 && !rend) {
+                    if (rbase < first) {
+                        rend = true;
+                        break;
+                    }
+                    const int p = rbase - lane;
+                    const bool st = p >= first && !(pk < key[idx[p]]);
+                    rmask = __ballot_sync(kFull, st);
+                    rchunk = rbase;
+                    rbase -= 32;
+                }
+                // the median of three leaves stoppers on both sides; running
+                // out of either means a broken invariant, reported as failure
+                if (rend) return false;
+                const int lpos = lend ? 0x7fffffff : lchunk + __ffs(lmask) - 1;
+                const int rpos = rchunk - (__ffs(rmask) - 1);
+                if (lpos < rpos) {
+                    if (lane == 0) {
+                        const int t = idx[lpos];
+                        idx[lpos] = idx[rpos];
+                        idx[rpos] = t;
+                    }
+                    __syncwarp();
+                    lmask &= lmask - 1;
+                    rmask &= rmask - 1;
+                    prev_r = rpos;
+                    continue;
+                }
+                cut = prev_r < 0 ? lpos : min(lpos, prev_r);
+                break;
+            }
+            __syncwarp();
+            if (cut >= last) return false;
+            if (cut < T) {
+                if (top >= cap) return false;
+                if (lane == 0) stack[top] = {cut, last, depth};
+                ++top;
+            }
+            last = cut;
+        }
+        if (first < T && last > prefix_end) prefix_end = last;
+    }
+    __syncwarp();
+    // insertion sort of [0, prefix_end) (at most a few dozen elements)
+    if (lane == 0) {
+        for (int i = 1; i < prefix_end; ++i) {
+            const int v = idx[i];
+            const float kv = key[v];
+            int j = i;
+            while (j > 0 && kv < key[idx[j - 1]]) {
+                idx[j] = idx[j - 1];
+                --j;
+            }
+            idx[j] = v;
+        }
+    }
+    __syncwarp();
+    return true;
+}
+
 template <int D>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) ksg_tie_kernel(KsgTieArgs A) {
+    __shared__ SortSegment s_stack[kWarpsPerCta][kStack];
     const int lane = threadIdx.x & 31;
     const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     float* dz = A.dz + warp * A.stride;
@@ -127,12 +258,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) ksg_tie_kernel(KsgTieArgs A
             idx[j] = j;
         }
         __syncwarp();
-        int ok = 1;
-        if (lane == 0) {
-            SortSegment stack[kStack];
-            ok = sort_prefix_like_reference(dz, idx, m, A.k + 1, stack, kStack) ? 1 : 0;
-        }
-        ok = __shfl_sync(kFull, ok, 0);
+        const int ok = sort_prefix_warp(dz, idx, m, A.k + 1, s_stack[threadIdx.x >> 5], kStack, lane) ? 1 : 0;
         __syncwarp();
         if (!ok) {
             if (lane == 0) atomicOr(A.fault, FAULT_TIE_UNRESOLVED);
