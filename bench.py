@@ -395,10 +395,13 @@ def main():
         # the counts 2d (d, d-1, 1), counted by the kernels
         evs = [plans[s].evaluations() for s in range(args.warmup, S)]
         exec_ops = statistics.mean(e[0] * 4 * DIM + e[1] * 2 * DIM for e in evs)
+        evals = {"joint": statistics.mean(e[0] for e in evs),
+                 "one_variable": statistics.mean(e[1] for e in evs)}
         kernel = "ksg_grid_pass1_kernel + ksg_grid_count_kernel"
         traffic = GRID_DRAM_BYTES_PER_PAIR * B if m == M_FRAMES else None
     else:
         exec_ops = ops_launch
+        evals = None
         kernel = "ksg_count_kernel"
         traffic = None
     achieved = exec_ops / avg_launch_s / 1e9
@@ -552,7 +555,7 @@ def main():
                          "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
                                             "256-pair step, scaled by pairs" if traffic else None),
                          "kernel": kernel, "search": search,
-                         "ops_per_launch": exec_ops,
+                         "ops_per_launch": exec_ops, "evaluations_per_launch": evals,
                          "exhaustive_ops_per_launch": ops_launch,
                          "effective_gops": effective,
                          "peak_source": (f"{props.multi_processor_count} SMs x 128 lanes x "
