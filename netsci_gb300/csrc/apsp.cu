@@ -7,17 +7,27 @@
 // minimum of single roundings, so the result does not depend on the order k
 // is visited in and matches the CPU restatement bit for bit.
 //
-// Kernel shape: a 128 x 64 output tile per CTA of 256 threads, 8 x 4 outputs
-// per thread (about 80 registers, three CTAs per SM), k in slabs of 16
-// staged in shared memory as interleaved pairs
-// (k, k+1), so one packed add (add.rn.f32x2) forms two candidate sums and one
-// three-input min folds both into the running minimum: two instructions per
-// two (i, j, k) terms. The work is FADD/FMNMX issue-bound on CUDA cores; a
-// min-plus product has no tensor-core form.
+// The iterate is kept transposed, X = H^T, so both operands of a step are
+// contiguous along k:
+//     Xn[j][i] = Hn[i][j] = min_k fl(X[i][k] + A[j][k]).
+// X and a copy of A live in P x P buffers (P = n rounded up to 128, +inf
+// outside n x n, so padded k contribute nothing and no load needs a bound
+// check); the result is transposed back into H once at the end.
 //
-// Convergence: step t writes changed[t] = 1 when any entry differs from H;
-// step t+1 returns at once when changed[t] == 0 (H is then a fixed point and
-// both buffers hold it).
+// Kernel shape: a 128 x 64 output tile per CTA of 256 threads, 8 x 4 outputs
+// per thread (two CTAs per SM). k runs in slabs of 16: both operand tiles
+// (128 and 64 rows of 16 floats) are copied into shared memory with 16-byte
+// cp.async into two buffers, so the next slab loads while this one is
+// reduced. Rows are padded to 20 floats, which keeps the 16-byte reads of a
+// quarter-warp on distinct banks. Each thread reads four consecutive k of a
+// row at once; one packed add (add.rn.f32x2) forms the sums for (k, k+1) and
+// one three-input min folds both into the running minimum: two instructions
+// per two (i, j, k) terms. The work is FADD/FMNMX issue-bound on CUDA cores;
+// a min-plus product has no tensor-core form.
+//
+// Convergence: step t writes changed[t] = 1 when any entry differs from the
+// previous iterate; step t+1 returns at once when changed[t] == 0 (the
+// iterate is then a fixed point and both buffers hold it).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,28 +39,52 @@
 namespace nsg {
 namespace {
 
-constexpr int kTileI = 128;  // output rows i per CTA
-constexpr int kTileJ = 64;   // output columns j per CTA
-constexpr int kSlab = 16;    // k values per stage (8 pairs)
+constexpr int kTileI = 128;  // output rows i per CTA (rows of X)
+constexpr int kTileJ = 64;   // output columns j per CTA (rows of A)
+constexpr int kSlab = 16;    // k values per stage
+constexpr int kRow = 20;     // shared-memory row stride (floats)
 constexpr int kThreads = 256;
-constexpr int kHLoads = (kSlab * kTileI) / kThreads;  // elements per thread per slab
-constexpr int kALoads = (kSlab * kTileJ) / kThreads;
+constexpr int kPad = 128;    // P is a multiple of this (and of kTileJ, kSlab)
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 __global__ void __launch_bounds__(kThreads, 2)
-hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
-                       float* __restrict__ Hn, int n, int* changed, int step) {
+hedetniemi_step_kernel(const float* __restrict__ X, const float* __restrict__ Ap,
+                       float* __restrict__ Xn, int n, int P, int* changed, int step) {
     if (step > 0 && changed[step - 1] == 0) return;  // fixed point reached earlier
-    __shared__ __align__(16) float2 Hs[kSlab / 2][kTileI];  // (H[k][i], H[k+1][i])
-    __shared__ __align__(16) float2 As[kSlab / 2][kTileJ];  // (A[j][k], A[j][k+1])
+    __shared__ __align__(16) float Xs[2][kTileI][kRow];
+    __shared__ __align__(16) float As[2][kTileJ][kRow];
     const float inf = __int_as_float(0x7f800000);
     const int tid = threadIdx.x;
-    // Rows i = i0 + 32w + 2tx + {0,1} for w = 0..3: the lanes of a warp read
-    // consecutive 16-byte pairs of Hs (no bank replays). Columns
-    // j = j0 + 32w + 2ty + {0,1} for w = 0..1: two addresses per warp.
+    // rows i = i0 + tx + 16u (u < 8), columns j = j0 + ty + 16v (v < 4)
     const int tx = tid & 15;
     const int ty = tid >> 4;
     const int i0 = blockIdx.y * kTileI;
     const int j0 = blockIdx.x * kTileJ;
+    const float* xg = X + (size_t)i0 * P;
+    const float* ag = Ap + (size_t)j0 * P;
+    // 128 + 64 rows of four 16-byte chunks: three chunks per thread
+    auto load_slab = [&](int buf, int k0) {
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            const int c = tid + kThreads * e;
+            if (c < 4 * kTileI) {
+                const int r = c >> 2, q = c & 3;
+                cp_async16(&Xs[buf][r][4 * q], xg + (size_t)r * P + k0 + 4 * q);
+            } else {
+                const int c2 = c - 4 * kTileI;
+                const int r = c2 >> 2, q = c2 & 3;
+                cp_async16(&As[buf][r][4 * q], ag + (size_t)r * P + k0 + 4 * q);
+            }
+        }
+        cp_async_commit();
+    };
 
     float acc[8][4];
 #pragma unroll
@@ -58,65 +92,83 @@ hedetniemi_step_kernel(const float* __restrict__ A, const float* __restrict__ H,
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = inf;
 
-    for (int k0 = 0; k0 < n; k0 += kSlab) {
-        __syncthreads();
-#pragma unroll
-        for (int e = 0; e < kHLoads; ++e) {
-            const int idx = e * kThreads + tid;
-            const int kk = idx / kTileI;
-            const int ii = idx - kk * kTileI;
-            const int k = k0 + kk, i = i0 + ii;
-            reinterpret_cast<float*>(&Hs[kk >> 1][ii])[kk & 1] =
-                (k < n && i < n) ? __ldg(H + (size_t)k * n + i) : inf;
-        }
-#pragma unroll
-        for (int e = 0; e < kALoads; ++e) {
-            const int idx = e * kThreads + tid;
-            const int jj = idx / kSlab;
-            const int kk = idx - jj * kSlab;
-            const int k = k0 + kk, j = j0 + jj;
-            reinterpret_cast<float*>(&As[kk >> 1][jj])[kk & 1] =
-                (k < n && j < n) ? __ldg(A + (size_t)j * n + k) : inf;
+    const int nslab = P / kSlab;
+    load_slab(0, 0);
+    for (int sl = 0; sl < nslab; ++sl) {
+        if (sl + 1 < nslab) {
+            load_slab((sl + 1) & 1, (sl + 1) * kSlab);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
+        const int b = sl & 1;
 #pragma unroll
-        for (int kp = 0; kp < kSlab / 2; ++kp) {
-            float2 h[8], a[4];
+        for (int kq = 0; kq < kSlab / 4; ++kq) {
+            float4 x[8], a[4];
 #pragma unroll
-            for (int w = 0; w < 4; ++w) {
-                h[2 * w] = Hs[kp][32 * w + 2 * tx];
-                h[2 * w + 1] = Hs[kp][32 * w + 2 * tx + 1];
-            }
+            for (int u = 0; u < 8; ++u) x[u] = *reinterpret_cast<const float4*>(&Xs[b][tx + 16 * u][4 * kq]);
 #pragma unroll
-            for (int w = 0; w < 2; ++w) {
-                a[2 * w] = As[kp][32 * w + 2 * ty];
-                a[2 * w + 1] = As[kp][32 * w + 2 * ty + 1];
-            }
+            for (int v = 0; v < 4; ++v) a[v] = *reinterpret_cast<const float4*>(&As[b][ty + 16 * v][4 * kq]);
 #pragma unroll
             for (int u = 0; u < 8; ++u)
 #pragma unroll
                 for (int v = 0; v < 4; ++v) {
-                    const float2 s = nsg_add2(a[v], h[u]);
-                    acc[u][v] = nsg_min3(acc[u][v], s.x, s.y);
+                    const float2 s0 = nsg_add2(make_float2(x[u].x, x[u].y), make_float2(a[v].x, a[v].y));
+                    const float2 s1 = nsg_add2(make_float2(x[u].z, x[u].w), make_float2(a[v].z, a[v].w));
+                    acc[u][v] = nsg_min3(acc[u][v], s0.x, s0.y);
+                    acc[u][v] = nsg_min3(acc[u][v], s1.x, s1.y);
                 }
         }
+        __syncthreads();  // the buffer is refilled two slabs on
     }
 
     bool diff = false;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-        const int i = i0 + 32 * (u >> 1) + 2 * tx + (u & 1);
+        const int i = i0 + tx + 16 * u;
         if (i >= n) continue;
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            const int j = j0 + 32 * (v >> 1) + 2 * ty + (v & 1);
+            const int j = j0 + ty + 16 * v;
             if (j >= n) continue;
-            const size_t o = (size_t)i * n + j;
-            if (__float_as_int(acc[u][v]) != __float_as_int(__ldg(H + o))) diff = true;
-            Hn[o] = acc[u][v];
+            const size_t o = (size_t)j * P + i;
+            if (__float_as_int(acc[u][v]) != __float_as_int(__ldg(X + o))) diff = true;
+            Xn[o] = acc[u][v];
         }
     }
     if (__syncthreads_or(diff) && tid == 0) changed[step] = 1;
+}
+
+// dst (P x P) = src (n x n, stride n) or its transpose, +inf outside n x n.
+__global__ void pad_copy_kernel(const float* __restrict__ src, float* __restrict__ dst, int n, int P,
+                                int transpose) {
+    __shared__ float t[32][33];
+    const float inf = __int_as_float(0x7f800000);
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;  // dst tile: rows by.., columns bx..
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        const int sr = transpose ? bx + yy : by + yy;
+        const int sc = transpose ? by + threadIdx.x : bx + threadIdx.x;
+        t[yy][threadIdx.x] = (sr < n && sc < n) ? __ldg(src + (size_t)sr * n + sc) : inf;
+    }
+    __syncthreads();
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        const int r = by + yy, c = bx + threadIdx.x;
+        dst[(size_t)r * P + c] = transpose ? t[threadIdx.x][yy] : t[yy][threadIdx.x];
+    }
+}
+
+// H (n x n) = the n x n corner of X (stride P), transposed.
+__global__ void unpad_transpose_kernel(const float* __restrict__ X, float* __restrict__ H, int n, int P) {
+    __shared__ float t[32][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;  // H tile: rows by.., columns bx..
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y)
+        t[yy][threadIdx.x] = __ldg(X + (size_t)(bx + yy) * P + by + threadIdx.x);
+    __syncthreads();
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        const int r = by + yy, c = bx + threadIdx.x;
+        if (r < n && c < n) H[(size_t)r * n + c] = t[threadIdx.x][yy];
+    }
 }
 
 // Back-walk of netcalc/src/hedetniemi_gpu.cu:70-107 over snapshots Hi[p]
@@ -169,10 +221,20 @@ __global__ void corr_to_adj_kernel(const float* __restrict__ C, float* __restric
     A[idx] = v;
 }
 
-void launch_step(const float* A, const float* H, float* Hn, int n, int* changed, int step,
+void launch_step(const float* Ap, const float* X, float* Xn, int n, int P, int* changed, int step,
                  cudaStream_t s) {
-    dim3 grid((n + kTileJ - 1) / kTileJ, (n + kTileI - 1) / kTileI);
-    hedetniemi_step_kernel<<<grid, kThreads, 0, s>>>(A, H, Hn, n, changed, step);
+    dim3 grid(P / kTileJ, P / kTileI);
+    hedetniemi_step_kernel<<<grid, kThreads, 0, s>>>(X, Ap, Xn, n, P, changed, step);
+    NSG_CUDA(cudaGetLastError());
+}
+
+void launch_pad(const float* src, float* dst, int n, int P, bool transpose, cudaStream_t s) {
+    pad_copy_kernel<<<dim3(P / 32, P / 32), dim3(32, 8), 0, s>>>(src, dst, n, P, transpose ? 1 : 0);
+    NSG_CUDA(cudaGetLastError());
+}
+
+void launch_unpad(const float* X, float* H, int n, int P, cudaStream_t s) {
+    unpad_transpose_kernel<<<dim3((n + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, s>>>(X, H, n, P);
     NSG_CUDA(cudaGetLastError());
 }
 
@@ -189,17 +251,36 @@ struct DevMem {
     DevMem& operator=(const DevMem&) = delete;
 };
 
+// Padded copy of A and the two transposed iterates X = H^T, both starting at A^T.
+struct Iterates {
+    int P;
+    DevMem mem;
+    float* Ap;
+    float* X[2];
+    Iterates(const float* A, int n, cudaStream_t s)
+        : P((n + kPad - 1) / kPad * kPad), mem(sizeof(float) * 3 * (size_t)P * P, s) {
+        const size_t pp = (size_t)P * P;
+        Ap = static_cast<float*>(mem.p);
+        X[0] = Ap + pp;
+        X[1] = Ap + 2 * pp;
+        launch_pad(A, Ap, n, P, false, s);
+        launch_pad(A, X[0], n, P, true, s);
+        launch_pad(A, X[1], n, P, true, s);
+    }
+};
+
 }  // namespace
 
 int apsp_lengths(const float* A, float* H, int n, int max_path_length, cudaStream_t s) {
     if (n < 0 || max_path_length < 0) invalid("negative size or path length");
     const size_t nn = (size_t)n * n;
-    NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    if (max_path_length == 0 || n == 0) return 0;
-    DevMem tmp(nn * sizeof(float), s);
+    if (max_path_length == 0 || n == 0) {
+        NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        return 0;
+    }
+    Iterates it(A, n, s);
     DevMem changed(sizeof(int) * max_path_length, s);
     NSG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int) * max_path_length, s));
-    float* buf[2] = {H, static_cast<float*>(tmp.p)};
     int* ch = static_cast<int*>(changed.p);
     // Launch in chunks; read the last step's flag between chunks so long runs
     // stop shortly after the fixed point instead of queueing empty steps.
@@ -208,7 +289,7 @@ int apsp_lengths(const float* A, float* H, int n, int max_path_length, cudaStrea
     int last_flag = 1;
     while (t < max_path_length && last_flag) {
         const int end = std::min(max_path_length, t + chunk);
-        for (; t < end; ++t) launch_step(A, buf[t & 1], buf[(t + 1) & 1], n, ch, t, s);
+        for (; t < end; ++t) launch_step(it.Ap, it.X[t & 1], it.X[(t + 1) & 1], n, it.P, ch, t, s);
         NSG_CUDA(cudaMemcpyAsync(&last_flag, ch + (t - 1), sizeof(int), cudaMemcpyDeviceToHost, s));
         NSG_CUDA(cudaStreamSynchronize(s));
     }
@@ -222,11 +303,9 @@ int apsp_lengths(const float* A, float* H, int n, int max_path_length, cudaStrea
             break;
         }
     }
-    // Result lives in buf[t & 1]; when converged both buffers hold it.
-    if (buf[t & 1] != H) {
-        NSG_CUDA(cudaMemcpyAsync(H, buf[t & 1], nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
-        NSG_CUDA(cudaStreamSynchronize(s));
-    }
+    // The result lives in X[t & 1]; when converged both buffers hold it.
+    launch_unpad(it.X[t & 1], H, n, it.P, s);
+    NSG_CUDA(cudaStreamSynchronize(s));
     return steps;
 }
 
@@ -236,21 +315,16 @@ void apsp_paths(const float* A, float* H, int* paths, int n, int L, float tolera
     const size_t nn = (size_t)n * n;
     NSG_CUDA(cudaMemsetAsync(paths, 0xff, sizeof(int) * nn * L, s));  // -1
     if (n == 0) return;
-    DevMem tmp(nn * sizeof(float), s);
+    Iterates it(A, n, s);
     DevMem snaps(nn * L * sizeof(float), s);
     DevMem changed(sizeof(int) * L, s);
     NSG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int) * L, s));
-    NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    float* buf[2] = {H, static_cast<float*>(tmp.p)};
     float* Hi = static_cast<float*>(snaps.p);
     for (int p = 0; p < L; ++p) {
-        NSG_CUDA(cudaMemcpyAsync(Hi + nn * p, buf[p & 1], nn * sizeof(float),
-                                 cudaMemcpyDeviceToDevice, s));
-        launch_step(A, buf[p & 1], buf[(p + 1) & 1], n, static_cast<int*>(changed.p), p, s);
+        launch_unpad(it.X[p & 1], Hi + nn * p, n, it.P, s);  // H before step p
+        launch_step(it.Ap, it.X[p & 1], it.X[(p + 1) & 1], n, it.P, static_cast<int*>(changed.p), p, s);
     }
-    if (buf[L & 1] != H) {
-        NSG_CUDA(cudaMemcpyAsync(H, buf[L & 1], nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    }
+    launch_unpad(it.X[L & 1], H, n, it.P, s);
     dim3 block(32, 8);
     dim3 grid((n + 31) / 32, (n + 7) / 8);
     hedetniemi_walk_kernel<<<grid, block, 0, s>>>(H, Hi, A, paths, tolerance, n, L);
