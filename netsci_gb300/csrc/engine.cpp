@@ -547,8 +547,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
         n.G = grid_cells_per_axis(m);
         nodes.push_back(n);
         node_off.push_back(arena);
-        const size_t cells = static_cast<size_t>(n.G) * n.G + 1;
-        arena += align16(2 * kGridMaxG * sizeof(float)) + align16(cells * sizeof(int)) +
+        arena += align16(2 * kGridMaxG * sizeof(float)) + grid_index_bytes(n.G) +
                  align16(static_cast<size_t>(m) * sizeof(unsigned short)) +
                  align16(static_cast<size_t>(m) * sizeof(int)) +
                  align16(static_cast<size_t>(d_) * m * sizeof(float));
@@ -565,12 +564,11 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
     for (size_t i = 0; i < nodes.size(); ++i) {
         GridNode& n = nodes[i];
         unsigned char* q = base + node_off[i];
-        const size_t cells = static_cast<size_t>(n.G) * n.G + 1;
         n.e1 = reinterpret_cast<float*>(q);
         n.e2 = n.e1 + kGridMaxG;
         q += align16(2 * kGridMaxG * sizeof(float));
         n.start = reinterpret_cast<int*>(q);
-        q += align16(cells * sizeof(int));
+        q += grid_index_bytes(n.G);
         n.cell = reinterpret_cast<unsigned short*>(q);
         q += align16(static_cast<size_t>(n.m) * sizeof(unsigned short));
         n.perm = reinterpret_cast<int*>(q);
@@ -592,9 +590,8 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
             wpre.push_back(acc);
             acc += (descs[p].m + 31) / 32;
             const int G = nodes[gps[p].a].G;
-            const size_t cells = static_cast<size_t>(G) * G + 1;
             gps[p].start = reinterpret_cast<int*>(off);
-            off += align16(cells * sizeof(int));
+            off += grid_index_bytes(G);
             gps[p].perm = reinterpret_cast<int*>(off);
             off += align16(static_cast<size_t>(descs[p].m) * sizeof(int));
             gps[p].sx = reinterpret_cast<float*>(off);

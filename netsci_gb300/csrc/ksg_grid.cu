@@ -74,6 +74,39 @@ __device__ void block_scan(const int* cnt, int* out, int n) {
     __syncthreads();
 }
 
+// Query order of a grid's cells (the layout is described in ksg_grid.h):
+// cnt[c] holds the frames of row-major cell c. The Z-order codes of a
+// Gp x Gp square (Gp = G rounded up to a power of two, at most 32) are
+// ranked, skipping cells outside G x G, and the counts accumulated in that
+// order. tmp1, tmp2: shared scratch of 1024 and 1025 ints.
+__device__ void build_query_order(const int* cnt, int G, int* start, int* tmp1, int* tmp2) {
+    int* qstart = start + grid_qoff(G);
+    unsigned short* qcell = reinterpret_cast<unsigned short*>(qstart + grid_qoff(G));
+    int Gp = 1;
+    while (Gp < G) Gp <<= 1;
+    const int ncode = Gp * Gp;
+    const int t = threadIdx.x;
+    int row = 0, col = 0;
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+        row |= ((t >> (2 * b + 1)) & 1) << b;
+        col |= ((t >> (2 * b)) & 1) << b;
+    }
+    const bool valid = t < ncode && row < G && col < G;
+    if (t < ncode) tmp1[t] = valid ? 1 : 0;
+    __syncthreads();
+    block_scan(tmp1, tmp2, ncode);
+    const int rank = t < ncode ? tmp2[t] : 0;
+    __syncthreads();
+    if (valid) {
+        qcell[rank] = static_cast<unsigned short>(row * G + col);
+        tmp1[rank] = cnt[row * G + col];
+    }
+    __syncthreads();
+    block_scan(tmp1, tmp2, G * G);
+    for (int c = t; c <= G * G; c += blockDim.x) qstart[c] = tmp2[c];
+}
+
 // One CTA per node: axes, quantile edges, cells, counting sort by cell.
 template <int D>
 __global__ void __launch_bounds__(kPrepThreads) grid_node_kernel(GridNode* nodes) {
@@ -81,6 +114,7 @@ __global__ void __launch_bounds__(kPrepThreads) grid_node_kernel(GridNode* nodes
     __shared__ float s_e1[kGridMaxG], s_e2[kGridMaxG];
     __shared__ int s_cnt[kGridMaxG * kGridMaxG];
     __shared__ int s_start[kGridMaxG * kGridMaxG + 1];
+    __shared__ int s_tmp1[kGridMaxG * kGridMaxG], s_tmp2[kGridMaxG * kGridMaxG + 1];
     __shared__ int s_axis[2];
     GridNode nd = nodes[blockIdx.x];
     const int m = nd.m, G = nd.G, t = threadIdx.x;
@@ -144,6 +178,8 @@ __global__ void __launch_bounds__(kPrepThreads) grid_node_kernel(GridNode* nodes
             nd.sx[static_cast<long long>(c) * m + pos] = __ldg(nd.x + static_cast<long long>(c) * nd.ld + j);
         }
     }
+    __syncthreads();
+    build_query_order(s_cnt, G, nd.start, s_tmp1, s_tmp2);
 }
 
 // One CTA per pair of the batch: cells over (bin of a on its c1, bin of b on
@@ -154,6 +190,7 @@ __global__ void __launch_bounds__(kPrepThreads) grid_pair_kernel(const KsgPairDe
                                                                 const GridNode* nodes) {
     __shared__ int s_cnt[kGridMaxG * kGridMaxG];
     __shared__ int s_start[kGridMaxG * kGridMaxG + 1];
+    __shared__ int s_tmp1[kGridMaxG * kGridMaxG], s_tmp2[kGridMaxG * kGridMaxG + 1];
     const KsgPairDesc P = pairs[blockIdx.x];
     const GridPair gp = gps[blockIdx.x];
     const GridNode na = nodes[gp.a], nb = nodes[gp.b];
@@ -180,6 +217,8 @@ __global__ void __launch_bounds__(kPrepThreads) grid_pair_kernel(const KsgPairDe
                 __ldg(P.xb + static_cast<long long>(c) * P.ld + j);
         }
     }
+    __syncthreads();
+    build_query_order(s_cnt, G, gp.start, s_tmp1, s_tmp2);
 }
 
 // psi[n_x] + psi[n_y] per sample from the raw counts (self included), as

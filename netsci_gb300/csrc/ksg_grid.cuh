@@ -22,12 +22,13 @@
 //     with the two nodes' edges, both nodes' coordinates copied in that
 //     order with the frames' original indices.
 //
-// Warps, not CTAs, own queries: a warp takes 32 consecutive frames of the
-// pair grid (or node grid) as its queries, so their boxes overlap, and
+// Warps, not CTAs, own queries: a warp takes 32 frames consecutive in the
+// grid's query order (Z order of the cells) as its queries, so their boxes
+// overlap, and
 // streams the frames of the cells it must visit through its own slice of
 // shared memory, 128 frames at a time, read back as float4 broadcasts.
-// Pass 1 first scans the cells its queries sit in (the seed, which fills
-// the neighbour lists and bounds U), then cell rows outward from there,
+// Pass 1 first scans the rectangle of cells its queries sit in (the seed,
+// which fills the neighbour lists and bounds U), then cell rows outward,
 // recomputing each row's column range from the current bounds and stopping
 // in a direction at the first row no query can reach (rows further out have
 // bounds further away). The counts use the fixed eps and visit the row and
@@ -100,6 +101,21 @@ __device__ __forceinline__ void item_of(const int* wprefix, int npairs, int t, i
     }
     p = lo;
     blk = t - __ldg(wprefix + lo);
+}
+
+// Position (row-major storage) of the query of rank qi in a grid's query
+// order: the last query-order cell starting at or before qi (it is not
+// empty), then the offset within it.
+__device__ __forceinline__ int query_position(const int* start, int G, int qi) {
+    const int* qs = start + grid_qoff(G);
+    const unsigned short* qc = reinterpret_cast<const unsigned short*>(qs + grid_qoff(G));
+    int lo = 0, hi = G * G - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(qs + mid) <= qi) lo = mid;
+        else hi = mid - 1;
+    }
+    return __ldg(start + __ldg(qc + lo)) + (qi - __ldg(qs + lo));
 }
 
 // Stage frames [base, base+n) of a sorted grid (planes of `stride` floats)
@@ -200,14 +216,15 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
         if (t >= total) return;
         int p, blk;
         item_of(A.wprefix, A.npairs, t, p, blk);
-        const KsgPairDesc P = A.pairs[p];
+        const KsgPairDesc* P = A.pairs + p;  // fields read where used
         const GridPair gp = A.gp[p];
         const GridNode na = A.nodes[gp.a];
         const GridNode nb = A.nodes[gp.b];
-        const int m = P.m, G = na.G;
+        const int m = P->m, G = na.G;
         const long long st = m;
-        const int r = blk * 32 + lane;
-        const bool valid = r < m;
+        const int qi = blk * 32 + lane;  // query rank in the grid's query order
+        const bool valid = qi < m;
+        const int r = valid ? query_position(gp.start, G, qi) : 0;
         const int i = valid ? __ldg(gp.perm + r) : 0;
         float qa[D], qb[D];
 #pragma unroll
@@ -223,30 +240,38 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
             bd[s] = s < nsent ? -inf_f() : inf_f();
             bj[s] = -1;
         }
-        // cells of this warp's queries: pair cell = bin of a on c1, bin of b on c1
-        int my_cell = 0x7fffffff, my_cell_hi = -1;
-        if (valid) {
-            my_cell = (__ldg(na.cell + i) / G) * G + __ldg(nb.cell + i) / G;
-            my_cell_hi = my_cell;
+        // cells of this warp's queries: row = bin of a on c1, column = bin of b on c1
+        const int qrow = valid ? __ldg(na.cell + i) / G : 0;
+        const int qcol = valid ? __ldg(nb.cell + i) / G : 0;
+        const int rmin = __reduce_min_sync(0xffffffffu, valid ? qrow : G);
+        const int rmax = __reduce_max_sync(0xffffffffu, valid ? qrow : -1);
+        const int cmin = __reduce_min_sync(0xffffffffu, valid ? qcol : G);
+        const int cmax = __reduce_max_sync(0xffffffffu, valid ? qcol : -1);
+        // The seed is the rectangle of cells the queries span; where the
+        // query order jumps between distant blocks, the cell of the first
+        // query alone.
+        int srow_lo = rmin, srow_hi = rmax, scol_lo = cmin, scol_hi = cmax;
+        if ((rmax - rmin + 1) * (cmax - cmin + 1) > 16) {
+            srow_lo = srow_hi = __shfl_sync(0xffffffffu, qrow, 0);
+            scol_lo = scol_hi = __shfl_sync(0xffffffffu, qcol, 0);
         }
-        const int cell_lo = warp_min(my_cell);
-        const int cell_hi = warp_max(my_cell_hi);
-        const int seed_lo = __ldg(gp.start + cell_lo);
-        const int seed_hi = __ldg(gp.start + cell_hi + 1);
+        // the seed rectangle packed in one register (bins are below 256)
+        const unsigned seedbox = static_cast<unsigned>(srow_lo) | static_cast<unsigned>(srow_hi) << 8 |
+                                 static_cast<unsigned>(scol_lo) << 16 | static_cast<unsigned>(scol_hi) << 24;
         const float qa1 = qa[na.c1], qb1 = qb[nb.c1];
         // Ranges to scan, produced by a small state machine so that the scan
         // body (with its unrolled list inserts) exists once in the kernel:
-        // the seed, then the rows the queries sit in, then rows outward.
-        // Every query lies below row `up` (above row `dn`), so row `up` can
-        // only be reached across its lower edge, and if no query reaches that
-        // edge now, no row further up can be reached later (bounds only
-        // shrink). A row's range minus the seed interval may leave two pieces.
-        const int row_first = cell_lo / G, row_last = cell_hi / G;
-        int phase = 0;               // 0 seed, 1 the queries' rows, 2 outward
-        int cx = row_first, up = row_last + 1, dn = row_first - 1;
+        // the seed rows, then the rows the queries sit in (minus the seeded
+        // columns), then rows outward. Every query lies below row `up`
+        // (above row `dn`), so row `up` can only be reached across its lower
+        // edge, and if no query reaches that edge now, no row further up can
+        // be reached later (bounds only shrink). A row minus the seeded
+        // columns may leave two pieces.
+        int phase = 0;  // 0 seed rows, 1 the queries' rows, 2 outward
+        int cx = srow_lo, up = rmax + 1, dn = rmin - 1;
         bool prefer_up = true;
         int pend_lo = 0, pend_hi = 0;
-        long long scanned = 0;
+        int scanned = 0;  // at most m: a frame is scanned once per warp
         for (;;) {
             int lo, hi;
             if (pend_hi > pend_lo) {
@@ -254,14 +279,17 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
                 hi = pend_hi;
                 pend_hi = pend_lo;
             } else if (phase == 0) {
-                lo = seed_lo;
-                hi = seed_hi;
-                phase = 1;
+                lo = __ldg(gp.start + cx * G + (seedbox >> 16 & 0xff));
+                hi = __ldg(gp.start + cx * G + (seedbox >> 24) + 1);
+                if (++cx > static_cast<int>(seedbox >> 8 & 0xff)) {
+                    phase = 1;
+                    cx = dn + 1;  // rmin: dn moves only in phase 2
+                }
             } else {
                 const float u = valid ? bd[KMAX - 1] : -inf_f();
                 int row = -1;
                 if (phase == 1) {
-                    if (cx <= row_last) row = cx++;
+                    if (cx <= rmax) row = cx++;
                     else phase = 2;
                 }
                 if (phase == 2) {
@@ -278,26 +306,27 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
                 if (!__any_sync(0xffffffffu, reach)) continue;
                 int clo = G, chi = -1;
                 if (reach) bin_range(nb.e1, G, qb1, u, clo, chi);
-                clo = warp_min(clo);
-                chi = warp_max(chi);
+                clo = __reduce_min_sync(0xffffffffu, clo);
+                chi = __reduce_max_sync(0xffffffffu, chi);
                 if (clo > chi) continue;
-                const int ra = __ldg(gp.start + row * G + clo);
-                const int rb = __ldg(gp.start + row * G + chi + 1);
-                if (rb <= seed_lo || ra >= seed_hi) {
-                    lo = ra;
-                    hi = rb;
-                } else if (ra < seed_lo) {
-                    lo = ra;
-                    hi = seed_lo;
-                    if (rb > seed_hi) {
-                        pend_lo = seed_hi;
-                        pend_hi = rb;
+                int alo = clo, ahi = chi, blo = 1, bhi = 0;
+                if (row >= static_cast<int>(seedbox & 0xff) && row <= static_cast<int>(seedbox >> 8 & 0xff)) {
+                    ahi = min(chi, static_cast<int>(seedbox >> 16 & 0xff) - 1);
+                    blo = max(clo, static_cast<int>(seedbox >> 24) + 1);
+                    bhi = chi;
+                    if (alo > ahi) {
+                        alo = blo;
+                        ahi = bhi;
+                        blo = 1;
+                        bhi = 0;
                     }
-                } else if (rb > seed_hi) {
-                    lo = seed_hi;
-                    hi = rb;
-                } else {
-                    continue;
+                    if (alo > ahi) continue;
+                }
+                lo = __ldg(gp.start + row * G + alo);
+                hi = __ldg(gp.start + row * G + ahi + 1);
+                if (blo <= bhi) {
+                    pend_lo = __ldg(gp.start + row * G + blo);
+                    pend_hi = __ldg(gp.start + row * G + bhi + 1);
                 }
             }
             scanned += hi - lo;
@@ -321,11 +350,11 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
             for (int s = 1; s < KMAX - 1; ++s) {
                 const int j = bj[s];
                 if (s > nsent && j >= 0 && j < m) {
-                    ea = fmaxf(ea, ksgk::marginal_at<D>(qa, P.xa, P.ld, j));
-                    eb = fmaxf(eb, ksgk::marginal_at<D>(qb, P.xb, P.ld, j));
+                    ea = fmaxf(ea, ksgk::marginal_at<D>(qa, P->xa, P->ld, j));
+                    eb = fmaxf(eb, ksgk::marginal_at<D>(qb, P->xb, P->ld, j));
                 }
             }
-            const long long o = P.scratch + i;
+            const long long o = P->scratch + i;
             A.eps_a[o] = ea;
             A.eps_b[o] = eb;
             if (A.eps_x) A.eps_x[o] = ea;
@@ -342,7 +371,8 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
 
 // ---- pass 2: marginal counts on a node grid -------------------------------------
 // A work item is a count group (up to kCountGroup pairs that count the same
-// node's variable) and a block of 32 queries consecutive in that node's grid;
+// node's variable) and a block of 32 queries consecutive in that node grid's
+// query order;
 // the warp visits the union of the queries' boxes for the largest of the
 // pairs' eps and counts every pair from one distance per frame.
 template <int D>
@@ -366,8 +396,9 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
         int* out = grp.side ? A.cnt_b : A.cnt_a;
         const int m = nd.m, G = nd.G;
         const long long st = m;
-        const int r = blk * 32 + lane;
-        const bool valid = r < m;
+        const int qi = blk * 32 + lane;  // query rank in the node grid's query order
+        const bool valid = qi < m;
+        const int r = valid ? query_position(nd.start, G, qi) : 0;
         const int i = valid ? __ldg(nd.perm + r) : 0;
         float q[D];
 #pragma unroll

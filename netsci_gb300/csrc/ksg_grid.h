@@ -14,6 +14,20 @@ constexpr int kGridMaxG = 32;
 constexpr int kGridChunk = 128;     // frames staged per warp step
 constexpr int kGridWarps = 8;       // warps per CTA
 
+// Cell index of a grid, one block of memory at `start`:
+//   start[G*G+1]   first position of each cell, cells row-major (b1*G + b2);
+//   qstart[G*G+1]  the same counts accumulated in query order;
+//   qcell[G*G]     row-major cell of the t-th cell in query order.
+// Query order is the Z (Morton) order of (b1, b2): a warp's 32 queries, taken
+// consecutively in that order, sit in a compact block of cells rather than
+// along one row, so the union of their search boxes is smaller. Frames stay
+// stored row-major, which keeps a row's column range contiguous.
+__host__ __device__ inline int grid_qoff(int G) { return (G * G + 1 + 3) & ~3; }
+inline size_t grid_index_bytes(int G) {
+    return sizeof(int) * 2 * static_cast<size_t>(grid_qoff(G)) +
+           ((static_cast<size_t>(G) * G * sizeof(unsigned short) + 15) & ~static_cast<size_t>(15));
+}
+
 // Node grid of one trajectory row (device descriptor).
 struct GridNode {
     const float* x;        // original row: x[c*ld + j]
@@ -23,7 +37,7 @@ struct GridNode {
     float* e2;             // likewise along c2 (all +inf when c2 < 0)
     unsigned short* cell;  // [m] cell of frame j: b1*G + b2
     int* perm;             // [m] frames in cell order
-    int* start;            // [G*G+1] first position of each cell
+    int* start;            // cell index (grid_index_bytes(G)), see above
     float* sx;             // [d][m] coordinates in cell order (plane stride m)
 };
 
@@ -31,7 +45,7 @@ struct GridNode {
 struct GridPair {
     int a, b;              // node indices
     int* perm;             // [m] frames in pair-cell order
-    int* start;            // [G*G+1]
+    int* start;            // cell index (grid_index_bytes(G)), see above
     float* sx;             // [2d][m] coordinates of a then b in that order
 };
 

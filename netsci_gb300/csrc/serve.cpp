@@ -87,7 +87,7 @@ size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 // sorted coordinates) for m samples of d coordinates.
 size_t node_grid_bytes(int m, int d) {
     const int G = grid_cells_per_axis(m);
-    return align16(2 * kGridMaxG * sizeof(float)) + align16((static_cast<size_t>(G) * G + 1) * sizeof(int)) +
+    return align16(2 * kGridMaxG * sizeof(float)) + grid_index_bytes(G) +
            align16(static_cast<size_t>(m) * sizeof(unsigned short)) + align16(static_cast<size_t>(m) * sizeof(int)) +
            align16(static_cast<size_t>(d) * m * sizeof(float));
 }
@@ -99,12 +99,11 @@ GridNode node_grid_at(unsigned char* base, const float* x, int ld, int m) {
     n.ld = ld;
     n.m = m;
     n.G = grid_cells_per_axis(m);
-    const size_t cells = static_cast<size_t>(n.G) * n.G + 1;
     n.e1 = reinterpret_cast<float*>(base);
     n.e2 = n.e1 + kGridMaxG;
     base += align16(2 * kGridMaxG * sizeof(float));
     n.start = reinterpret_cast<int*>(base);
-    base += align16(cells * sizeof(int));
+    base += grid_index_bytes(n.G);
     n.cell = reinterpret_cast<unsigned short*>(base);
     base += align16(static_cast<size_t>(m) * sizeof(unsigned short));
     n.perm = reinterpret_cast<int*>(base);
@@ -429,7 +428,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
             g.b = j->slots[q].second;
             const int G = grid_cells_per_axis(pr.m);
             g.start = reinterpret_cast<int*>(arena);
-            arena += align16((static_cast<size_t>(G) * G + 1) * sizeof(int));
+            arena += grid_index_bytes(G);
             g.perm = reinterpret_cast<int*>(arena);
             arena += align16(static_cast<size_t>(pr.m) * sizeof(int));
             g.sx = reinterpret_cast<float*>(arena);
