@@ -80,17 +80,6 @@ __device__ __forceinline__ void bin_range(const float* e, int G, float q, float 
     hi = a;
 }
 
-__device__ __forceinline__ int warp_min(int v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ int warp_max(int v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
 // Pair index and warp block of work item t (binary search over wprefix).
 __device__ __forceinline__ void item_of(const int* wprefix, int npairs, int t, int& p, int& blk) {
     int lo = 0, hi = npairs - 1;
@@ -372,9 +361,9 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
 // ---- pass 2: marginal counts on a node grid -------------------------------------
 // A work item is a count group (up to kCountGroup pairs that count the same
 // node's variable) and a block of 32 queries consecutive in that node grid's
-// query order;
-// the warp visits the union of the queries' boxes for the largest of the
-// pairs' eps and counts every pair from one distance per frame.
+// query order. The warp visits the union of the queries' boxes for the
+// largest of the pairs' eps, row by row over the columns of the boxes that
+// hold the row, and counts every pair from one distance per frame.
 template <int D>
 __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArgs A) {
     using namespace gridk;
@@ -414,20 +403,24 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
         }
         const float q1 = q[nd.c1];
         const float q2 = nd.c2 >= 0 ? q[nd.c2] : 0.f;
-        int rlo = G, rhi = -1, clo = G, chi = -1;
+        // each query's box of rows [qrlo, qrhi] and columns [qclo, qchi];
+        // a row is scanned over the columns of the queries whose box holds it
+        int qrlo = G, qrhi = -1, qclo = G, qchi = -1;
         if (valid) {
-            bin_range(nd.e1, G, q1, emax, rlo, rhi);
-            bin_range(nd.e2, G, q2, emax, clo, chi);
+            bin_range(nd.e1, G, q1, emax, qrlo, qrhi);
+            bin_range(nd.e2, G, q2, emax, qclo, qchi);
         }
-        rlo = warp_min(rlo);
-        rhi = warp_max(rhi);
-        clo = warp_min(clo);
-        chi = warp_max(chi);
+        const int rlo = __reduce_min_sync(0xffffffffu, qrlo);
+        const int rhi = __reduce_max_sync(0xffffffffu, qrhi);
         int cnt[kCountGroup];
 #pragma unroll
         for (int p = 0; p < kCountGroup; ++p) cnt[p] = 0;
         long long scanned = 0;
-        for (int cx = rlo; cx <= rhi && clo <= chi; ++cx) {
+        for (int cx = rlo; cx <= rhi; ++cx) {
+            const bool in_row = cx >= qrlo && cx <= qrhi;
+            const int clo = __reduce_min_sync(0xffffffffu, in_row ? qclo : G);
+            const int chi = __reduce_max_sync(0xffffffffu, in_row ? qchi : -1);
+            if (clo > chi) continue;
             const int lo = __ldg(nd.start + cx * G + clo);
             const int hi = __ldg(nd.start + cx * G + chi + 1);
             scanned += hi - lo;
