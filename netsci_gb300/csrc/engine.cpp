@@ -708,8 +708,6 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         t.dz = tie_dz_.as<float>();
         t.idx = tie_idx_.as<int>();
         t.stride = tie_stride_;
-        t.gp = g.gps.as<GridPair>();
-        t.nodes = g.nodes.as<GridNode>();
         ksg_launch_ties(t, d_, s);
         KsgFinalArgs f{};
         f.pairs = bp;

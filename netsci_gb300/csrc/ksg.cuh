@@ -39,9 +39,6 @@ struct KsgTie {
     float wk;             // its k-th (= (k+1)-th) joint distance
 };
 
-struct GridPair;
-struct GridNode;
-
 struct KsgCountArgs {
     const KsgPairDesc* pairs;
     const KsgItem* items;
@@ -79,11 +76,6 @@ struct KsgTieArgs {
     float* dz;            // per-warp scratch rows of `stride` floats
     int* idx;             // per-warp scratch rows of `stride` ints
     long long stride;
-    // cell grids of the pairs (same indexing as pairs), or null: a tie whose
-    // frames at distance wk all have the same marginals is then found on the
-    // grid and left as the search computed it
-    const GridPair* gp;
-    const GridNode* nodes;
 };
 
 struct KsgFinalArgs {

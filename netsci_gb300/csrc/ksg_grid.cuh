@@ -185,6 +185,34 @@ __device__ __forceinline__ void count_chunk(const float* tile, int n, const floa
     }
 }
 
+// Tie check over a staged chunk (2d planes): the range of each marginal over
+// the frames whose joint distance equals w (w < 0: no tie, nothing matches).
+template <int D>
+__device__ __forceinline__ void tie_chunk(const float* tile, int n, const float (&qa)[D], const float (&qb)[D],
+                                          float w, float& lo_a, float& hi_a, float& lo_b, float& hi_b) {
+    const int ngroups = (n + 3) >> 2;
+    for (int g = 0; g < ngroups; ++g) {
+        float4 ga[D], gb[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            ga[c] = *reinterpret_cast<const float4*>(tile + c * kGridChunk + 4 * g);
+            gb[c] = *reinterpret_cast<const float4*>(tile + (D + c) * kGridChunk + 4 * g);
+        }
+        float da[4], db[4];
+        ksgk::Marg<D, 1>::four(qa, ga, da);
+        ksgk::Marg<D, 1>::four(qb, gb, db);
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            if (fmaxf(da[f], db[f]) == w) {
+                lo_a = fminf(lo_a, da[f]);
+                hi_a = fmaxf(hi_a, da[f]);
+                lo_b = fminf(lo_b, db[f]);
+                hi_b = fmaxf(hi_b, db[f]);
+            }
+        }
+    }
+}
+
 }  // namespace gridk
 
 // ---- pass 1: joint k nearest neighbours, eps, ties -----------------------------
@@ -332,9 +360,9 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
         }
         // eps from list positions 1..k (original rows), tie test
         float ea = 0.f, eb = 0.f;
-        bool tie = false;
+        const float wk = bd[KMAX - 2];
+        bool tie = valid && wk == bd[KMAX - 1] && wk > 0.f;
         if (valid) {
-            tie = bd[KMAX - 2] == bd[KMAX - 1] && bd[KMAX - 2] > 0.f;
 #pragma unroll
             for (int s = 1; s < KMAX - 1; ++s) {
                 const int j = bj[s];
@@ -348,10 +376,49 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
             A.eps_b[o] = eb;
             if (A.eps_x) A.eps_x[o] = ea;
             if (A.eps_y) A.eps_y[o] = eb;
-            if (A.kdist) A.kdist[o] = bd[KMAX - 2];
+            if (A.kdist) A.kdist[o] = wk;
+        }
+        if (__any_sync(0xffffffffu, tie)) {
+            // Frames at distance wk lie in the cells within wk of the sample.
+            // When they all have the same marginal pair, whichever of them the
+            // reference's sort puts first gives the same eps, and the search's
+            // result stands; only the others go to the tie kernel. Resampled
+            // trajectories (bootstrap) tie on a large share of samples, nearly
+            // all between copies of one frame.
+            int qrlo = G, qrhi = -1, qclo = G, qchi = -1;
             if (tie) {
-                const int slot = atomicAdd(A.tie_count, 1);
-                if (slot < A.tie_cap) A.ties[slot] = KsgTie{A.pair_base + p, i, bd[KMAX - 2]};
+                bin_range(na.e1, G, qa1, wk, qrlo, qrhi);
+                bin_range(nb.e1, G, qb1, wk, qclo, qchi);
+            }
+            const int rlo = __reduce_min_sync(0xffffffffu, qrlo);
+            const int rhi = __reduce_max_sync(0xffffffffu, qrhi);
+            float lo_a = inf_f(), hi_a = -inf_f(), lo_b = inf_f(), hi_b = -inf_f();
+            for (int cx = rlo; cx <= rhi; ++cx) {
+                const bool in_row = cx >= qrlo && cx <= qrhi;
+                const int clo = __reduce_min_sync(0xffffffffu, in_row ? qclo : G);
+                const int chi = __reduce_max_sync(0xffffffffu, in_row ? qchi : -1);
+                if (clo > chi) continue;
+                const int lo = __ldg(gp.start + cx * G + clo);
+                const int hi = __ldg(gp.start + cx * G + chi + 1);
+                for (int base = lo; base < hi; base += kGridChunk) {
+                    const int n = min(kGridChunk, hi - base);
+                    __syncwarp();
+                    stage<2 * D, false>(tile, nullptr, gp.sx, st, nullptr, base, n, lane);
+                    __syncwarp();
+                    tie_chunk<D>(tile, n, qa, qb, tie ? wk : -1.f, lo_a, hi_a, lo_b, hi_b);
+                }
+            }
+            tie = tie && !(lo_a == hi_a && lo_b == hi_b);
+        }
+        // tied samples of the warp take consecutive slots of the tie list
+        const unsigned tmask = __ballot_sync(0xffffffffu, tie);
+        if (tmask) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(A.tie_count, __popc(tmask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (tie) {
+                const int slot = base + __popc(tmask & ((1u << lane) - 1u));
+                if (slot < A.tie_cap) A.ties[slot] = KsgTie{A.pair_base + p, i, wk};
                 else atomicOr(A.fault, FAULT_TIE_OVERFLOW);
             }
         }

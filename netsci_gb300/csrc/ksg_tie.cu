@@ -3,13 +3,16 @@
 // A sample whose k-th and (k+1)-th nearest joint distances are equal (and
 // non-zero) has a neighbour set that the reference CPU path picks by the
 // order its std::sort leaves equal distances in
-// (netcalc/src/mutual_information_cpu.cpp:48-77). The count kernel appends
-// such samples to a list; this kernel takes them one warp at a time:
+// (netcalc/src/mutual_information_cpu.cpp:48-77). The search kernels append
+// such samples to a list, unless every frame at the tied distance has the same
+// marginal pair (then any order gives the same eps); this kernel takes the list
+// one warp at a time:
 //
 //   1. the warp writes the sample's full joint-distance row (the reference's
 //      arithmetic) and the identity index array into its scratch rows;
-//   2. lane 0 replays the reference sort's order on the prefix that holds
-//      the neighbours (sort_prefix.h);
+//   2. the warp replays the reference sort's order on the prefix that holds
+//      the neighbours (the steps sort_prefix.h restates, partitions found 32
+//      elements at a time with ballots);
 //   3. the lanes holding sorted positions 1..k compute eps_a / eps_b, a warp
 //      max-reduction combines them;
 //   4. the marginal counts are recounted over all frames with warp ballots
@@ -21,7 +24,6 @@
 #include "common.cuh"
 #include "engine.h"
 #include "ksg.cuh"
-#include "ksg_grid.cuh"
 #include "sort_prefix.h"
 
 namespace nsg {
@@ -210,47 +212,6 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) ksg_tie_kernel(KsgTieArgs A
         for (int c = 0; c < D; ++c) {
             qa[c] = __ldg(xa + (size_t)c * ld + sq);
             qb[c] = __ldg(xb + (size_t)c * ld + sq);
-        }
-        if (A.gp) {
-            // Frames at distance wk lie in the cells within wk of the sample;
-            // when they all have the same marginal pair, whichever of them
-            // the reference's sort puts first gives the same eps, and the
-            // search's result stands.
-            const GridPair gp = A.gp[t.pair];
-            const GridNode na = A.nodes[gp.a], nb = A.nodes[gp.b];
-            const int G = na.G;
-            const long long st = m;
-            const float u = t.wk;
-            int rlo, rhi, clo, chi;
-            gridk::bin_range(na.e1, G, qa[na.c1], u, rlo, rhi);
-            gridk::bin_range(nb.e1, G, qb[nb.c1], u, clo, chi);
-            float lo_a = __int_as_float(0x7f800000), hi_a = -lo_a, lo_b = lo_a, hi_b = -lo_a;
-            for (int cx = rlo; cx <= rhi && clo <= chi; ++cx) {
-                const int r1 = __ldg(gp.start + cx * G + chi + 1);
-                for (int r = __ldg(gp.start + cx * G + clo) + lane; r < r1; r += 32) {
-                    float da = fabsf(qa[0] - __ldg(gp.sx + r));
-                    float db = fabsf(qb[0] - __ldg(gp.sx + D * st + r));
-#pragma unroll
-                    for (int c = 1; c < D; ++c) {
-                        da = fmaxf(da, fabsf(qa[c] - __ldg(gp.sx + c * st + r)));
-                        db = fmaxf(db, fabsf(qb[c] - __ldg(gp.sx + (D + c) * st + r)));
-                    }
-                    if (fmaxf(da, db) == u) {
-                        lo_a = fminf(lo_a, da);
-                        hi_a = fmaxf(hi_a, da);
-                        lo_b = fminf(lo_b, db);
-                        hi_b = fmaxf(hi_b, db);
-                    }
-                }
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                lo_a = fminf(lo_a, __shfl_xor_sync(kFull, lo_a, off));
-                hi_a = fmaxf(hi_a, __shfl_xor_sync(kFull, hi_a, off));
-                lo_b = fminf(lo_b, __shfl_xor_sync(kFull, lo_b, off));
-                hi_b = fmaxf(hi_b, __shfl_xor_sync(kFull, hi_b, off));
-            }
-            if (lo_a == hi_a && lo_b == hi_b) continue;
         }
         for (int j = lane; j < m; j += 32) {
             const int s = tie_frame(fmap, j, ld, A.fault);

@@ -514,8 +514,6 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     t.dz = d_tie_dz_.as<float>();
     t.idx = d_tie_idx_.as<int>();
     t.stride = cfg_.max_m;
-    t.gp = d_gpairs_.as<GridPair>();
-    t.nodes = d_gnodes_.as<GridNode>();
     ksg_launch_ties_ctas(t, d, kServeTieCtas, s);
     for (size_t si = 0; si < slices.size(); ++si) {
         Job* j = slices[si].first;
