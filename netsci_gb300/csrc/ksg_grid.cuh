@@ -125,11 +125,15 @@ __device__ __forceinline__ void stage(float* tile, int* jt, const float* sx, lon
     }
 }
 
-// Pass 1 over a staged chunk: frames' original indices in jt.
-template <int D, int KMAX>
+// Pass 1 over a staged chunk: frames' original indices in jt. The list holds
+// the KL nearest frames other than the query itself: the first frame at
+// distance 0 stands for the query (self_seen) and is not listed. Frames at
+// distance 0 have both marginal distances 0, so which of them is left out
+// changes neither eps nor the counts.
+template <int D, int KL>
 __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, int n,
                                             const float (&qa)[D], const float (&qb)[D],
-                                            float (&bd)[KMAX], int (&bj)[KMAX]) {
+                                            float (&bd)[KL], int (&bj)[KL], bool& self_seen) {
     const int ngroups = (n + 3) >> 2;
     for (int g = 0; g < ngroups; ++g) {
         float4 ga[D], gb[D];
@@ -144,7 +148,7 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
 #pragma unroll
         for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
         const float mn = nsg_min3(dz[0], dz[1], fminf(dz[2], dz[3]));
-        if (mn < bd[KMAX - 1]) {
+        if (mn < bd[KL - 1]) {
             // In a pruned scan most frames are near the queries, so some lane
             // of the warp inserts in a large share of groups. Insert each
             // lane's nearest frame of the group first, in one shared step;
@@ -157,10 +161,14 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
                 vm = lt ? dz[f] : vm;
                 fm = lt ? f : fm;
             }
-            ksgk::list_insert<KMAX>(bd, bj, mn, jt[4 * g + fm]);
+            if (mn == 0.f && !self_seen) self_seen = true;
+            else ksgk::list_insert<KL>(bd, bj, mn, jt[4 * g + fm]);
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
-                if (f != fm && dz[f] < bd[KMAX - 1]) ksgk::list_insert<KMAX>(bd, bj, dz[f], jt[4 * g + f]);
+                if (f != fm && dz[f] < bd[KL - 1]) {
+                    if (dz[f] == 0.f && !self_seen) self_seen = true;
+                    else ksgk::list_insert<KL>(bd, bj, dz[f], jt[4 * g + f]);
+                }
             }
         }
     }
@@ -249,11 +257,15 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
             qa[c] = valid ? __ldg(gp.sx + c * st + r) : 0.f;
             qb[c] = valid ? __ldg(gp.sx + (D + c) * st + r) : 0.f;
         }
-        float bd[KMAX];
-        int bj[KMAX];
+        // the k + 1 nearest frames other than the query, after nsent -inf
+        // sentinels (list positions 1..k+1 of the reference's sorted row)
+        constexpr int KL = KMAX - 1;
+        float bd[KL];
+        int bj[KL];
+        bool self_seen = false;
         const int nsent = KMAX - (A.k + 2);
 #pragma unroll
-        for (int s = 0; s < KMAX; ++s) {
+        for (int s = 0; s < KL; ++s) {
             bd[s] = s < nsent ? -inf_f() : inf_f();
             bj[s] = -1;
         }
@@ -303,7 +315,7 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
                     cx = dn + 1;  // rmin: dn moves only in phase 2
                 }
             } else {
-                const float u = valid ? bd[KMAX - 1] : -inf_f();
+                const float u = valid ? bd[KL - 1] : -inf_f();
                 int row = -1;
                 if (phase == 1) {
                     if (cx <= rmax) row = cx++;
@@ -352,7 +364,7 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
                 __syncwarp();
                 stage<2 * D, true>(tile, jt, gp.sx, st, gp.perm, base, n, lane);
                 __syncwarp();
-                pass1_chunk<D, KMAX>(tile, jt, n, qa, qb, bd, bj);
+                pass1_chunk<D, KL>(tile, jt, n, qa, qb, bd, bj, self_seen);
             }
         }
         if (A.evals && lane == 0) {
@@ -360,13 +372,13 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
         }
         // eps from list positions 1..k (original rows), tie test
         float ea = 0.f, eb = 0.f;
-        const float wk = bd[KMAX - 2];
-        bool tie = valid && wk == bd[KMAX - 1] && wk > 0.f;
+        const float wk = bd[KL - 2];
+        bool tie = valid && wk == bd[KL - 1] && wk > 0.f;
         if (valid) {
 #pragma unroll
-            for (int s = 1; s < KMAX - 1; ++s) {
+            for (int s = 0; s < KL - 1; ++s) {
                 const int j = bj[s];
-                if (s > nsent && j >= 0 && j < m) {
+                if (s >= nsent && j >= 0 && j < m) {
                     ea = fmaxf(ea, ksgk::marginal_at<D>(qa, P->xa, P->ld, j));
                     eb = fmaxf(eb, ksgk::marginal_at<D>(qb, P->xb, P->ld, j));
                 }
