@@ -126,14 +126,32 @@ __device__ __forceinline__ void stage(float* tile, int* jt, const float* sx, lon
 }
 
 // Pass 1 over a staged chunk: frames' original indices in jt. The list holds
-// the KL nearest frames other than the query itself: the first frame at
-// distance 0 stands for the query (self_seen) and is not listed. Frames at
+// the KN nearest frames other than the query itself, sorted; its last entry U
+// bounds admission (a frame enters when strictly nearer). The first frame at
+// distance 0 stands for the query (self_seen) and is not listed: frames at
 // distance 0 have both marginal distances 0, so which of them is left out
-// changes neither eps nor the counts.
-template <int D, int KL>
+// changes neither eps nor the counts. `tied` records whether some frame
+// outside the list lies at distance exactly U: one rejected at U, or evicted
+// while U stayed the same. U only decreases, and no frame outside the list
+// can lie at a new, smaller U, so a decrease clears the flag.
+template <int D, int KN>
+__device__ __forceinline__ void admit(float (&bd)[KN], int (&bj)[KN], bool& self_seen, bool& tied,
+                                      float v, int j) {
+    const float u = bd[KN - 1];
+    if (v == 0.f && !self_seen) {
+        self_seen = true;
+    } else if (v < u) {
+        ksgk::list_insert<KN>(bd, bj, v, j);
+        tied = bd[KN - 1] == u;
+    } else {
+        tied = true;  // v == u
+    }
+}
+
+template <int D, int KN>
 __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, int n,
                                             const float (&qa)[D], const float (&qb)[D],
-                                            float (&bd)[KL], int (&bj)[KL], bool& self_seen) {
+                                            float (&bd)[KN], int (&bj)[KN], bool& self_seen, bool& tied) {
     const int ngroups = (n + 3) >> 2;
     for (int g = 0; g < ngroups; ++g) {
         float4 ga[D], gb[D];
@@ -148,11 +166,11 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
 #pragma unroll
         for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
         const float mn = nsg_min3(dz[0], dz[1], fminf(dz[2], dz[3]));
-        if (mn < bd[KL - 1]) {
+        if (mn <= bd[KN - 1]) {
             // In a pruned scan most frames are near the queries, so some lane
             // of the warp inserts in a large share of groups. Insert each
             // lane's nearest frame of the group first, in one shared step;
-            // it lowers the threshold, so the other frames rarely still pass.
+            // it lowers the bound, so the other frames rarely still pass.
             int fm = 0;
             float vm = dz[0];
 #pragma unroll
@@ -161,14 +179,10 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
                 vm = lt ? dz[f] : vm;
                 fm = lt ? f : fm;
             }
-            if (mn == 0.f && !self_seen) self_seen = true;
-            else ksgk::list_insert<KL>(bd, bj, mn, jt[4 * g + fm]);
+            admit<D, KN>(bd, bj, self_seen, tied, mn, jt[4 * g + fm]);
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
-                if (f != fm && dz[f] < bd[KL - 1]) {
-                    if (dz[f] == 0.f && !self_seen) self_seen = true;
-                    else ksgk::list_insert<KL>(bd, bj, dz[f], jt[4 * g + f]);
-                }
+                if (f != fm && dz[f] <= bd[KN - 1]) admit<D, KN>(bd, bj, self_seen, tied, dz[f], jt[4 * g + f]);
             }
         }
     }
@@ -257,12 +271,12 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
             qa[c] = valid ? __ldg(gp.sx + c * st + r) : 0.f;
             qb[c] = valid ? __ldg(gp.sx + (D + c) * st + r) : 0.f;
         }
-        // the k + 1 nearest frames other than the query, after nsent -inf
-        // sentinels (list positions 1..k+1 of the reference's sorted row)
-        constexpr int KL = KMAX - 1;
+        // the k nearest frames other than the query, after nsent -inf
+        // sentinels (list positions 1..k of the reference's sorted row)
+        constexpr int KL = KMAX - 2;
         float bd[KL];
         int bj[KL];
-        bool self_seen = false;
+        bool self_seen = false, tied = false;
         const int nsent = KMAX - (A.k + 2);
 #pragma unroll
         for (int s = 0; s < KL; ++s) {
@@ -364,7 +378,7 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
                 __syncwarp();
                 stage<2 * D, true>(tile, jt, gp.sx, st, gp.perm, base, n, lane);
                 __syncwarp();
-                pass1_chunk<D, KL>(tile, jt, n, qa, qb, bd, bj, self_seen);
+                pass1_chunk<D, KL>(tile, jt, n, qa, qb, bd, bj, self_seen, tied);
             }
         }
         if (A.evals && lane == 0) {
@@ -372,11 +386,12 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
         }
         // eps from list positions 1..k (original rows), tie test
         float ea = 0.f, eb = 0.f;
-        const float wk = bd[KL - 2];
-        bool tie = valid && wk == bd[KL - 1] && wk > 0.f;
+        // wk: the k-th distance; a tie when another frame lies at wk too
+        const float wk = bd[KL - 1];
+        bool tie = valid && tied && wk > 0.f;
         if (valid) {
 #pragma unroll
-            for (int s = 0; s < KL - 1; ++s) {
+            for (int s = 0; s < KL; ++s) {
                 const int j = bj[s];
                 if (s >= nsent && j >= 0 && j < m) {
                     ea = fmaxf(ea, ksgk::marginal_at<D>(qa, P->xa, P->ld, j));
