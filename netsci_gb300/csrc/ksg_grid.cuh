@@ -126,28 +126,8 @@ __device__ __forceinline__ void stage(float* tile, int* jt, const float* sx, lon
 }
 
 // Pass 1 over a staged chunk: frames' original indices in jt. The list holds
-// the KN nearest frames other than the query itself, sorted; its last entry U
-// bounds admission (a frame enters when strictly nearer). The first frame at
-// distance 0 stands for the query (self_seen) and is not listed: frames at
-// distance 0 have both marginal distances 0, so which of them is left out
-// changes neither eps nor the counts. `tied` records whether some frame
-// outside the list lies at distance exactly U: one rejected at U, or evicted
-// while U stayed the same. U only decreases, and no frame outside the list
-// can lie at a new, smaller U, so a decrease clears the flag.
-template <int D, int KN>
-__device__ __forceinline__ void admit(float (&bd)[KN], int (&bj)[KN], bool& self_seen, bool& tied,
-                                      float v, int j) {
-    const float u = bd[KN - 1];
-    if (v == 0.f && !self_seen) {
-        self_seen = true;
-    } else if (v < u) {
-        ksgk::list_insert<KN>(bd, bj, v, j);
-        tied = bd[KN - 1] == u;
-    } else {
-        tied = true;  // v == u
-    }
-}
-
+// the KN nearest frames other than the query itself, with the flag `tied`
+// for a frame outside it at the k-th distance (ksgk::admit).
 template <int D, int KN>
 __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, int n,
                                             const float (&qa)[D], const float (&qb)[D],
@@ -179,10 +159,10 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
                 vm = lt ? dz[f] : vm;
                 fm = lt ? f : fm;
             }
-            admit<D, KN>(bd, bj, self_seen, tied, mn, jt[4 * g + fm]);
+            ksgk::admit<KN>(bd, bj, self_seen, tied, mn, jt[4 * g + fm]);
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
-                if (f != fm && dz[f] <= bd[KN - 1]) admit<D, KN>(bd, bj, self_seen, tied, dz[f], jt[4 * g + f]);
+                if (f != fm && dz[f] <= bd[KN - 1]) ksgk::admit<KN>(bd, bj, self_seen, tied, dz[f], jt[4 * g + f]);
             }
         }
     }

@@ -10,9 +10,10 @@
 //     (structure-of-arrays: one row of `frames` floats per coordinate plane),
 //     reads frames four at a time as float4 broadcasts, and forms the joint
 //     Chebyshev distance dz = max(d_a, d_b). A per-sample ascending list of
-//     the k+2 smallest (dz, j) -- the sample itself, whose dz is 0, and its
-//     k+1 nearest -- lives in registers; it is only touched when the minimum
-//     dz of the four frames is below the list's last entry, which after the
+//     the k smallest (dz, j) over the frames other than the sample itself
+//     lives in registers, with a flag for a frame outside the list at the
+//     k-th distance (see admit()); it is only touched when the minimum dz of
+//     the four frames is at most the list's last entry, which after the
 //     first few hundred frames is rare, and then by one branch-free bubble
 //     step per candidate.
 //   * eps_a / eps_b are the largest marginal distances over list positions
@@ -23,18 +24,21 @@
 //   * The sample's psi[n_x] + psi[n_y] (float add, :110) goes to the pair's
 //     scratch row; ksg_final_kernel sums the row in sample order.
 //
-// Why the list needs no index tie-break: position 0 always holds a frame at
-// distance 0 (the sample itself or an exact duplicate, all with zero
-// marginals), and when the values at positions k and k+1 differ, positions
-// 1..k hold exactly the frames with dz <= that k-th value, whatever order
-// equal values were inserted in. When they are equal (and non-zero) the
+// Why the list needs no index tie-break: position 0 of the reference's sorted
+// row holds a frame at distance 0 (the sample itself or an exact duplicate,
+// all with zero marginals), and when the values at positions k and k+1
+// differ, positions 1..k hold exactly the frames with dz <= that k-th value,
+// whatever order equal values were offered in. Here position 0 is the first
+// zero-distance frame offered, left out of the list, and `tied` says whether
+// positions k and k+1 are equal. When they are (and non-zero) the
 // reference's choice depends on its sort; the sample goes to the tie list
 // and ksg_tie_kernel recomputes it. Frames past m are staged as +inf and
-// never pass the strict admission test.
+// are never offered.
 //
-// Runtime k with KMAX >= k+2: the first KMAX-k-2 slots hold -inf sentinels
-// that never move, so the live entries occupy the last k+2 slots and the
-// admission threshold is always slot KMAX-1 (a static register index).
+// Runtime k with KMAX >= k+2: the list has KN = KMAX-2 slots, the first
+// KN-k of them -inf sentinels that never move, so the live entries occupy the
+// last k slots and the admission bound is always slot KN-1 (a static
+// register index).
 //
 // Arithmetic: one rounded subtraction per coordinate, then exact abs/max, and
 // exact compares, so distances, eps and counts are bit-identical to the
@@ -66,6 +70,30 @@ __device__ __forceinline__ void list_insert(float (&bd)[KMAX], int (&bj)[KMAX], 
         bd[s] = hi;
         bj[s - 1] = jl;
         bj[s] = jh;
+    }
+}
+
+// Offer frame j at joint distance v to a sample's list of the KN nearest
+// frames other than the sample itself (sorted; the last entry U bounds
+// admission: a frame enters when strictly nearer). The first frame at
+// distance 0 stands for the sample (self_seen) and is not listed: frames at
+// distance 0 have both marginal distances 0, so which of them is left out
+// changes neither eps nor the counts. `tied` records whether a frame outside
+// the list lies at distance exactly U: one rejected at U, or evicted while U
+// stayed the same. U only decreases, and no frame outside the list can lie at
+// a new, smaller U, so a decrease clears the flag. Callers offer only frames
+// with v <= U.
+template <int KN>
+__device__ __forceinline__ void admit(float (&bd)[KN], int (&bj)[KN], bool& self_seen, bool& tied,
+                                      float v, int j) {
+    const float u = bd[KN - 1];
+    if (v == 0.f && !self_seen) {
+        self_seen = true;
+    } else if (v < u) {
+        list_insert<KN>(bd, bj, v, j);
+        tied = bd[KN - 1] == u;
+    } else {
+        tied = true;  // v == u
     }
 }
 
@@ -145,10 +173,11 @@ __device__ __forceinline__ float marginal_at(const float (&q)[D], const float* _
 
 // Pass 1 over one tile: planes of the tile at tile[c*stride + f], frames
 // j0 .. j0+jn-1 (frames past the pair's end hold +inf).
-template <int D, int KMAX, int R, int VARIANT>
+template <int D, int KN, int R, int VARIANT>
 __device__ __forceinline__ void pass1_tile(const float* tile, int stride, int j0, int jn,
                                            const float (&qa)[R][D], const float (&qb)[R][D],
-                                           float (&bd)[R][KMAX], int (&bj)[R][KMAX]) {
+                                           float (&bd)[R][KN], int (&bj)[R][KN], bool (&self_seen)[R],
+                                           bool (&tied)[R]) {
     const int ngroups = (jn + 3) >> 2;
     for (int g = 0; g < ngroups; ++g) {
         float4 ga[D], gb[D];
@@ -165,11 +194,11 @@ __device__ __forceinline__ void pass1_tile(const float* tile, int stride, int j0
 #pragma unroll
             for (int f = 0; f < 4; ++f) dz[f] = fmaxf(da[f], db[f]);
             const float mn = nsg_min3(dz[0], dz[1], fminf(dz[2], dz[3]));
-            if (mn < bd[r][KMAX - 1]) {
+            if (mn <= bd[r][KN - 1]) {
 #pragma unroll
                 for (int f = 0; f < 4; ++f) {
-                    if (dz[f] < bd[r][KMAX - 1]) {
-                        list_insert<KMAX>(bd[r], bj[r], dz[f], j0 + 4 * g + f);
+                    if (dz[f] <= bd[r][KN - 1]) {
+                        admit<KN>(bd[r], bj[r], self_seen[r], tied[r], dz[f], j0 + 4 * g + f);
                     }
                 }
             }
@@ -217,11 +246,12 @@ __device__ __forceinline__ void pass2_tile(const float* tile, int stride, int jn
 }
 
 // Query samples of this thread and their empty neighbour lists.
-template <int D, int KMAX, int R, int NT>
+template <int D, int KN, int R, int NT>
 __device__ __forceinline__ void load_queries(const KsgCountArgs& A, const KsgItem& w,
                                              const KsgPairDesc& P, int tid, float (&qa)[R][D],
                                              float (&qb)[R][D], int (&qi)[R],
-                                             float (&bd)[R][KMAX], int (&bj)[R][KMAX]) {
+                                             float (&bd)[R][KN], int (&bj)[R][KN], bool (&self_seen)[R],
+                                             bool (&tied)[R]) {
     const float kInf = __int_as_float(0x7f800000);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -234,34 +264,36 @@ __device__ __forceinline__ void load_queries(const KsgCountArgs& A, const KsgIte
             qb[r][c] = valid ? __ldg(P.xb + (size_t)c * P.ld + src) : 0.f;
         }
     }
-    // k+2 live entries: the sample itself (distance 0), the k nearest and
-    // the next one, so that a tie at the k-th distance is visible.
-    const int nsent = KMAX - (A.k + 2);
+    // k live entries after nsent -inf sentinels: the k nearest frames other
+    // than the sample (list positions 1..k of the reference's sorted row)
+    const int nsent = KN - A.k;
 #pragma unroll
-    for (int r = 0; r < R; ++r)
+    for (int r = 0; r < R; ++r) {
+        self_seen[r] = false;
+        tied[r] = false;
 #pragma unroll
-        for (int s = 0; s < KMAX; ++s) {
+        for (int s = 0; s < KN; ++s) {
             bd[r][s] = s < nsent ? -kInf : kInf;
             bj[r][s] = -1;
         }
+    }
 }
 
-// eps from list positions 1..k, and the tie test. Position p is slot
-// nsent+p; positions 1..k are slots nsent+1 .. KMAX-2 and position k+1 is
-// slot KMAX-1. A sample is flagged when its k-th distance equals its
-// (k+1)-th and is not zero: then the reference's choice among the frames at
-// that distance comes from its sort. (ra, rb) are the marginals of the
-// frame at position k; pass 2 checks whether every frame at distance wk has
-// the same ones (for example copies of one frame in a bootstrap resample),
-// in which case the choice cannot change eps and the flag is dropped.
-template <int D, int KMAX, int R>
+// eps from list positions 1..k (slots nsent .. KN-1), and the tie test: a
+// sample is flagged when another frame lies at its k-th distance wk (the flag
+// `tied`) and wk is not zero; then the reference's choice among the frames at
+// that distance comes from its sort. (ra, rb) are the marginals of the frame
+// at position k; pass 2 checks whether every frame at distance wk has the
+// same ones (for example copies of one frame in a bootstrap resample), in
+// which case the choice cannot change eps and the flag is dropped.
+template <int D, int KN, int R>
 __device__ __forceinline__ void eps_and_ties(const KsgCountArgs& A, const KsgItem& w,
                                              const KsgPairDesc& P, const float (&qa)[R][D],
                                              const float (&qb)[R][D], const int (&qi)[R],
-                                             const float (&bd)[R][KMAX], const int (&bj)[R][KMAX],
-                                             float (&ea)[R], float (&eb)[R], bool (&tie)[R],
-                                             float (&wk)[R], float (&ra)[R], float (&rb)[R]) {
-    const int nsent = KMAX - (A.k + 2);
+                                             const float (&bd)[R][KN], const int (&bj)[R][KN],
+                                             const bool (&tied)[R], float (&ea)[R], float (&eb)[R],
+                                             bool (&tie)[R], float (&wk)[R], float (&ra)[R], float (&rb)[R]) {
+    const int nsent = KN - A.k;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         ea[r] = 0.f;
@@ -269,18 +301,18 @@ __device__ __forceinline__ void eps_and_ties(const KsgCountArgs& A, const KsgIte
         ra[r] = 0.f;
         rb[r] = 0.f;
         const bool valid = qi[r] < w.q1;
-        wk[r] = bd[r][KMAX - 2];
-        tie[r] = valid && bd[r][KMAX - 2] == bd[r][KMAX - 1] && bd[r][KMAX - 2] > 0.f;
+        wk[r] = bd[r][KN - 1];
+        tie[r] = valid && tied[r] && wk[r] > 0.f;
 #pragma unroll
-        for (int s = 1; s < KMAX - 1; ++s) {
+        for (int s = 0; s < KN; ++s) {
             const int j = bj[r][s];
-            if (valid && s > nsent && j >= 0 && j < P.m) {
+            if (valid && s >= nsent && j >= 0 && j < P.m) {
                 const int src = frame_of(P.fmap, j, P.ld, A.fault);
                 const float da = marginal_at<D>(qa[r], P.xa, P.ld, src);
                 const float db = marginal_at<D>(qb[r], P.xb, P.ld, src);
                 ea[r] = fmaxf(ea[r], da);
                 eb[r] = fmaxf(eb[r], db);
-                if (s == KMAX - 2) {
+                if (s == KN - 1) {
                     ra[r] = da;
                     rb[r] = db;
                 }
@@ -308,10 +340,10 @@ __device__ __forceinline__ void report_ties(const KsgCountArgs& A, const KsgItem
     }
 }
 
-template <int KMAX, int R>
+template <int R>
 __device__ __forceinline__ void write_outputs(const KsgCountArgs& A, const KsgItem& w,
                                               const KsgPairDesc& P, const int (&qi)[R],
-                                              const float (&bd)[R][KMAX], const float (&ea)[R],
+                                              const float (&wk)[R], const float (&ea)[R],
                                               const float (&eb)[R], const int (&ca)[R],
                                               const int (&cb)[R]) {
 #pragma unroll
@@ -327,7 +359,7 @@ __device__ __forceinline__ void write_outputs(const KsgCountArgs& A, const KsgIt
             if (A.ny) A.ny[o] = ny;
             if (A.eps_x) A.eps_x[o] = ea[r];
             if (A.eps_y) A.eps_y[o] = eb[r];
-            if (A.kdist) A.kdist[o] = bd[r][KMAX - 2];
+            if (A.kdist) A.kdist[o] = wk[r];
         }
     }
 }
@@ -371,9 +403,11 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
 
         float qa[R][D], qb[R][D];
         int qi[R];
-        float bd[R][KMAX];
-        int bj[R][KMAX];
-        load_queries<D, KMAX, R, NT>(A, w, P, tid, qa, qb, qi, bd, bj);
+        constexpr int KN = KMAX - 2;
+        float bd[R][KN];
+        int bj[R][KN];
+        bool self_seen[R], tied[R];
+        load_queries<D, KN, R, NT>(A, w, P, tid, qa, qb, qi, bd, bj, self_seen, tied);
 
         const int ntiles = (m + J - 1) / J;
         // ---- pass 1: k nearest joint neighbours ------------------------------
@@ -382,11 +416,11 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
             __syncthreads();
             stage_tile<D, NT, J>(tile, P, j0, tid, A.fault);
             __syncthreads();
-            pass1_tile<D, KMAX, R, VARIANT>(&tile[0][0], J, j0, min(J, m - j0), qa, qb, bd, bj);
+            pass1_tile<D, KN, R, VARIANT>(&tile[0][0], J, j0, min(J, m - j0), qa, qb, bd, bj, self_seen, tied);
         }
         float ea[R], eb[R], wk[R], ra[R], rb[R];
         bool tie[R], mixed[R];
-        eps_and_ties<D, KMAX, R>(A, w, P, qa, qb, qi, bd, bj, ea, eb, tie, wk, ra, rb);
+        eps_and_ties<D, KN, R>(A, w, P, qa, qb, qi, bd, bj, tied, ea, eb, tie, wk, ra, rb);
         bool any_tie = false;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -419,7 +453,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
             }
         }
         report_ties<R>(A, w, qi, tie, mixed, wk);
-        write_outputs<KMAX, R>(A, w, P, qi, bd, ea, eb, ca, cb);
+        write_outputs<R>(A, w, P, qi, wk, ea, eb, ca, cb);
     }
 }
 
@@ -495,9 +529,11 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel_tma(KsgCountArgs A) {
 
         float qa[R][D], qb[R][D];
         int qi[R];
-        float bd[R][KMAX];
-        int bj[R][KMAX];
-        load_queries<D, KMAX, R, NT>(A, w, P, tid, qa, qb, qi, bd, bj);
+        constexpr int KN = KMAX - 2;
+        float bd[R][KN];
+        int bj[R][KN];
+        bool self_seen[R], tied[R];
+        load_queries<D, KN, R, NT>(A, w, P, tid, qa, qb, qi, bd, bj, self_seen, tied);
         float ea[R], eb[R], wk[R], ra[R], rb[R];
         bool tie[R], mixed[R];
         bool any_tie = false;
@@ -552,9 +588,9 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel_tma(KsgCountArgs A) {
                 __syncthreads();
             }
             if (v < T || T == 1) {
-                pass1_tile<D, KMAX, R, VARIANT>(tile, J, j0, jn, qa, qb, bd, bj);
+                pass1_tile<D, KN, R, VARIANT>(tile, J, j0, jn, qa, qb, bd, bj, self_seen, tied);
                 if (v == T - 1) {
-                    eps_and_ties<D, KMAX, R>(A, w, P, qa, qb, qi, bd, bj, ea, eb, tie, wk, ra, rb);
+                    eps_and_ties<D, KN, R>(A, w, P, qa, qb, qi, bd, bj, tied, ea, eb, tie, wk, ra, rb);
 #pragma unroll
                     for (int r = 0; r < R; ++r) any_tie |= tie[r];
                     any_tie = __any_sync(0xffffffffu, any_tie);
@@ -577,7 +613,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel_tma(KsgCountArgs A) {
             }
         }
         report_ties<R>(A, w, qi, tie, mixed, wk);
-        write_outputs<KMAX, R>(A, w, P, qi, bd, ea, eb, ca, cb);
+        write_outputs<R>(A, w, P, qi, wk, ea, eb, ca, cb);
     }
 }
 
