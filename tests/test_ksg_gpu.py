@@ -377,7 +377,7 @@ def test_bootstrap_duplicates_and_real_ties(oracle_mod):
     Xr = X.reshape(N, 3, m)[:, :, idx].reshape(N, 3 * m)
     expect = oracle_mod.pairs(Xr, m, 3, ab, k, gc=False, threads=8)
     # both searches: exhaustive (copies filtered in its count pass) and cell
-    # grids (resampled rows copied out; copies filtered by the tie kernel)
+    # grids (resampled rows copied out; copies filtered in the search pass)
     try:
         for mode, name in ((0, "exhaustive"), (1, "cell-grid")):
             device.set_ksg_search(mode)
