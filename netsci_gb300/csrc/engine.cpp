@@ -619,7 +619,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
             int acc = 0;
             for (size_t gi = first; gi < groups.size(); ++gi) {
                 gpre.push_back(acc);
-                acc += (nodes[groups[gi].node].m + 31) / 32;
+                acc += (nodes[groups[gi].node].m + kCountQueries - 1) / kCountQueries;
             }
             gpre.push_back(acc);
             g->ngroups.push_back(static_cast<int>(groups.size() - first));

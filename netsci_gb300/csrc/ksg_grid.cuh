@@ -80,6 +80,14 @@ __device__ __forceinline__ void bin_range(const float* e, int G, float q, float 
     hi = a;
 }
 
+// Largest of D non-negative values (three-input max for D = 3).
+template <int D>
+__device__ __forceinline__ float max_of(const float (&v)[D]) {
+    if constexpr (D == 1) return v[0];
+    else if constexpr (D == 2) return fmaxf(v[0], v[1]);
+    else return nsg_max3(v[0], v[1], v[2]);
+}
+
 // Pair index and warp block of work item t (binary search over wprefix).
 __device__ __forceinline__ void item_of(const int* wprefix, int npairs, int t, int& p, int& blk) {
     int lo = 0, hi = npairs - 1;
@@ -170,20 +178,24 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
 
 // Counts over a staged chunk for up to kCountGroup pairs at once: one
 // distance per frame, compared with each pair's eps (unused slots hold -inf).
+// Two lanes share a query: the lane of parity `half` takes frames 4g + 2*half
+// and 4g + 2*half + 1 of each group of four.
 template <int D>
-__device__ __forceinline__ void count_chunk(const float* tile, int n, const float (&q)[D],
+__device__ __forceinline__ void count_chunk(const float* tile, int n, int half, const float (&q)[D],
                                             const float (&e)[kCountGroup], int (&cnt)[kCountGroup]) {
     const int ngroups = (n + 3) >> 2;
     for (int g = 0; g < ngroups; ++g) {
-        float4 gq[D];
+        float dq0[D], dq1[D];
 #pragma unroll
-        for (int c = 0; c < D; ++c) gq[c] = *reinterpret_cast<const float4*>(tile + c * kGridChunk + 4 * g);
-        float dq[4];
-        ksgk::Marg<D, 1>::four(q, gq, dq);
+        for (int c = 0; c < D; ++c) {
+            const float2 x = *reinterpret_cast<const float2*>(tile + c * kGridChunk + 4 * g + 2 * half);
+            const float2 s2 = nsg_sub2(make_float2(q[c], q[c]), x);
+            dq0[c] = fabsf(s2.x);
+            dq1[c] = fabsf(s2.y);
+        }
+        const float d0 = max_of<D>(dq0), d1 = max_of<D>(dq1);
 #pragma unroll
-        for (int f = 0; f < 4; ++f)
-#pragma unroll
-            for (int p = 0; p < kCountGroup; ++p) cnt[p] += dq[f] <= e[p] ? 1 : 0;
+        for (int p = 0; p < kCountGroup; ++p) cnt[p] += (d0 <= e[p] ? 1 : 0) + (d1 <= e[p] ? 1 : 0);
     }
 }
 
@@ -434,8 +446,8 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
 
 // ---- pass 2: marginal counts on a node grid -------------------------------------
 // A work item is a count group (up to kCountGroup pairs that count the same
-// node's variable) and a block of 32 queries consecutive in that node grid's
-// query order. The warp visits the union of the queries' boxes for the
+// node's variable) and a block of kCountQueries queries consecutive in that
+// node grid's query order, two lanes per query. The warp visits the union of the queries' boxes for the
 // largest of the pairs' eps, row by row over the columns of the boxes that
 // hold the row, and counts every pair from one distance per frame.
 template <int D>
@@ -459,7 +471,8 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
         int* out = grp.side ? A.cnt_b : A.cnt_a;
         const int m = nd.m, G = nd.G;
         const long long st = m;
-        const int qi = blk * 32 + lane;  // query rank in the node grid's query order
+        const int half = lane & 1;  // two lanes per query
+        const int qi = blk * kCountQueries + (lane >> 1);  // query rank in the node grid's query order
         const bool valid = qi < m;
         const int r = valid ? query_position(nd.start, G, qi) : 0;
         const int i = valid ? __ldg(nd.perm + r) : 0;
@@ -503,17 +516,19 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
                 __syncwarp();
                 stage<D, false>(tile, nullptr, nd.sx, st, nullptr, base, n, lane);
                 __syncwarp();
-                count_chunk<D>(tile, n, q, e, cnt);
+                count_chunk<D>(tile, n, half, q, e, cnt);
             }
         }
-        if (valid) {
+#pragma unroll
+        for (int p = 0; p < kCountGroup; ++p) cnt[p] += __shfl_xor_sync(0xffffffffu, cnt[p], 1);
+        if (valid && half == 0) {
 #pragma unroll
             for (int p = 0; p < kCountGroup; ++p)
                 if (p < grp.npairs) out[o[p]] = cnt[p];
         }
         if (A.evals && lane == 0) {
-            atomicAdd(A.evals + 1,
-                      static_cast<unsigned long long>(scanned) * min(32, m - blk * 32) * grp.npairs);
+            atomicAdd(A.evals + 1, static_cast<unsigned long long>(scanned) *
+                                       min(kCountQueries, m - blk * kCountQueries) * grp.npairs);
         }
     }
 }

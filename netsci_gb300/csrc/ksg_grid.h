@@ -52,6 +52,9 @@ struct GridPair {
 // Pairs of a batch that count the same variable (node grid): their counts
 // share every distance evaluation.
 constexpr int kCountGroup = 4;
+// Queries per warp in the counts: two lanes per query, each taking every
+// other frame, so the union of the warp's query boxes is that of 16 queries.
+constexpr int kCountQueries = 16;
 struct CountGroup {
     int node;                      // node grid
     int side;                      // 0: variable a of the pairs, 1: variable b

@@ -466,7 +466,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     append_count_groups(h_gpairs_, static_cast<int>(np), groups);
     std::vector<int> gpre(groups.size() + 1, 0);
     for (size_t gi = 0; gi < groups.size(); ++gi) {
-        gpre[gi + 1] = gpre[gi] + (h_pairs_[groups[gi].pairs[0]].m + 31) / 32;
+        gpre[gi + 1] = gpre[gi] + (h_pairs_[groups[gi].pairs[0]].m + kCountQueries - 1) / kCountQueries;
     }
     NSG_CUDA(cudaMemcpyAsync(d_groups_.get(), groups.data(), sizeof(CountGroup) * groups.size(),
                              cudaMemcpyHostToDevice, s));
