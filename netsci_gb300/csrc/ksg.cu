@@ -8,21 +8,47 @@
 namespace nsg {
 namespace {
 
-// One thread per pair: the float sum of the pair's per-sample psi terms in
+// One warp per pair: the float sum of the pair's per-sample psi terms in
 // sample order, then the KSG formula and the generalized-correlation
 // transform, with the reference's operation order and precisions:
 //   netcalc/src/mutual_information_gpu.cu:1065-1074 (sum, divide, formula)
 //   netcalc/src/generalized_correlation_gpu.cpp:16-31 (transform in double)
 // The sum is sequential on purpose: it reproduces the reference's float
-// rounding sequence exactly, and costs about m dependent adds per pair.
-__global__ void ksg_final_kernel(KsgFinalArgs A) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+// rounding sequence exactly, about m dependent adds per pair. The warp copies
+// the row into shared memory a chunk at a time with coalesced loads, and
+// lane 0 adds the chunk from there, so the chain of adds waits on shared
+// memory rather than on a global load per term.
+constexpr int kFinalWarps = 8;
+constexpr int kFinalChunk = 1024;
+
+__global__ void __launch_bounds__(kFinalWarps * 32) ksg_final_kernel(KsgFinalArgs A) {
+    __shared__ __align__(16) float s_row[kFinalWarps][kFinalChunk];
+    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * kFinalWarps + (threadIdx.x >> 5);
     if (p >= A.npairs) return;
+    float* row = s_row[threadIdx.x >> 5];
     const KsgPairDesc P = A.pairs[p];
     const int m = P.m;
     const float* __restrict__ s = A.psum + P.scratch;
     float avg = 0.f;
-    for (int q = 0; q < m; ++q) avg = __fadd_rn(avg, __ldg(s + q));
+    for (int base = 0; base < m; base += kFinalChunk) {
+        const int n = min(kFinalChunk, m - base);
+        __syncwarp();
+        for (int q = lane; q < n; q += 32) row[q] = __ldg(s + base + q);
+        __syncwarp();
+        if (lane == 0) {
+            const int n4 = n & ~3;
+            for (int q = 0; q < n4; q += 4) {
+                const float4 v = *reinterpret_cast<const float4*>(row + q);
+                avg = __fadd_rn(avg, v.x);
+                avg = __fadd_rn(avg, v.y);
+                avg = __fadd_rn(avg, v.z);
+                avg = __fadd_rn(avg, v.w);
+            }
+            for (int q = n4; q < n; ++q) avg = __fadd_rn(avg, row[q]);
+        }
+    }
+    if (lane != 0) return;
     avg = __fdiv_rn(avg, static_cast<float>(m));
     const float inv_k = __double2float_rn(__ddiv_rn(1.0, static_cast<double>(static_cast<float>(A.k))));
     const float mi = __fsub_rn(__fsub_rn(__fadd_rn(__ldg(A.psi + m), __ldg(A.psi + A.k)), inv_k), avg);
@@ -115,9 +141,8 @@ void ksg_launch_counts(const KsgCountArgs& a, int d, int kmax, const KsgShape& s
 
 void ksg_launch_final(const KsgFinalArgs& a, cudaStream_t st) {
     if (a.npairs <= 0) return;
-    const int threads = 128;
-    const int grid = (a.npairs + threads - 1) / threads;
-    ksg_final_kernel<<<grid, threads, 0, st>>>(a);
+    const int grid = (a.npairs + kFinalWarps - 1) / kFinalWarps;
+    ksg_final_kernel<<<grid, kFinalWarps * 32, 0, st>>>(a);
     NSG_CUDA(cudaGetLastError());
 }
 
