@@ -19,34 +19,120 @@ namespace nsg {
 // ---------------------------------------------------------------------------
 // DeviceBuffer
 // ---------------------------------------------------------------------------
-DeviceBuffer::DeviceBuffer(size_t bytes) { reset(bytes); }
-DeviceBuffer::~DeviceBuffer() {
-    if (p_) cudaFree(p_);
+// Freed blocks are kept per device, keyed by size, and handed out again for
+// requests of at least half their size. A block is cached only after
+// cudaDeviceSynchronize, the same device-wide wait cudaFree performs, so no
+// kernel can still be using it when it is handed out. The cache holds at most
+// kBlockCacheBytes per device; when cudaMalloc fails, every cached block is
+// freed and the allocation retried.
+namespace {
+
+constexpr size_t kBlockCacheBytes = size_t(32) << 30;
+
+struct BlockCache {
+    std::mutex mu;
+    std::map<int, std::multimap<size_t, void*>> blocks;  // device -> size -> block
+    std::map<int, size_t> held;                           // device -> bytes cached
+};
+
+BlockCache& block_cache() {
+    static BlockCache* c = new BlockCache();  // never destroyed: no frees at exit
+    return *c;
 }
-DeviceBuffer::DeviceBuffer(DeviceBuffer&& o) noexcept : p_(o.p_), bytes_(o.bytes_) {
+
+}  // namespace
+
+void release_cached_device_blocks() {
+    BlockCache& c = block_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (auto& [dev, m] : c.blocks) {
+        cudaSetDevice(dev);
+        for (auto& [sz, p] : m) cudaFree(p);
+        m.clear();
+        c.held[dev] = 0;
+    }
+    cudaSetDevice(cur);
+}
+
+DeviceBuffer::DeviceBuffer(size_t bytes) { reset(bytes); }
+DeviceBuffer::~DeviceBuffer() { release(); }
+DeviceBuffer::DeviceBuffer(DeviceBuffer&& o) noexcept
+    : p_(o.p_), bytes_(o.bytes_), capacity_(o.capacity_), device_(o.device_) {
     o.p_ = nullptr;
     o.bytes_ = 0;
+    o.capacity_ = 0;
+    o.device_ = -1;
 }
 DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
     if (this != &o) {
-        if (p_) cudaFree(p_);
+        release();
         p_ = o.p_;
         bytes_ = o.bytes_;
+        capacity_ = o.capacity_;
+        device_ = o.device_;
         o.p_ = nullptr;
         o.bytes_ = 0;
+        o.capacity_ = 0;
+        o.device_ = -1;
     }
     return *this;
 }
+
+void DeviceBuffer::release() {
+    if (!p_) return;
+    BlockCache& c = block_cache();
+    int cur = -1;
+    cudaGetDevice(&cur);
+    bool cached = false;
+    if (cur == device_ && cudaDeviceSynchronize() == cudaSuccess) {
+        std::lock_guard<std::mutex> lock(c.mu);
+        if (c.held[device_] + capacity_ <= kBlockCacheBytes) {
+            c.blocks[device_].emplace(capacity_, p_);
+            c.held[device_] += capacity_;
+            cached = true;
+        }
+    }
+    if (!cached) cudaFree(p_);
+    p_ = nullptr;
+    bytes_ = 0;
+    capacity_ = 0;
+    device_ = -1;
+}
+
 void DeviceBuffer::reset(size_t bytes) {
-    if (p_) {
-        cudaFree(p_);
-        p_ = nullptr;
-        bytes_ = 0;
+    release();
+    if (!bytes) return;
+    int dev = 0;
+    NSG_CUDA(cudaGetDevice(&dev));
+    BlockCache& c = block_cache();
+    {
+        std::lock_guard<std::mutex> lock(c.mu);
+        auto& m = c.blocks[dev];
+        auto it = m.lower_bound(bytes);
+        if (it != m.end() && it->first / 2 <= bytes) {
+            p_ = it->second;
+            capacity_ = it->first;
+            c.held[dev] -= it->first;
+            m.erase(it);
+        }
     }
-    if (bytes) {
-        NSG_CUDA(cudaMalloc(&p_, bytes));
-        bytes_ = bytes;
+    if (!p_) {
+        cudaError_t e = cudaMalloc(&p_, bytes);
+        if (e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            release_cached_device_blocks();
+            e = cudaMalloc(&p_, bytes);
+        }
+        if (e != cudaSuccess) {
+            p_ = nullptr;
+            NSG_CUDA(e);
+        }
+        capacity_ = bytes;
     }
+    bytes_ = bytes;
+    device_ = dev;
 }
 
 // ---------------------------------------------------------------------------

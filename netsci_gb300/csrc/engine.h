@@ -14,7 +14,9 @@
 
 namespace nsg {
 
-// Device allocation owned by the library.
+// Device allocation owned by the library. Blocks come from, and go back to,
+// a per-device cache of freed blocks (see engine.cpp), so plans built call
+// after call with the same sizes do not map and unmap gigabytes each time.
 class DeviceBuffer {
 public:
     DeviceBuffer() = default;
@@ -31,9 +33,15 @@ public:
     void reset(size_t bytes);
 
 private:
+    void release();
     void* p_ = nullptr;
-    size_t bytes_ = 0;
+    size_t bytes_ = 0;     // requested
+    size_t capacity_ = 0;  // size of the block
+    int device_ = -1;
 };
+
+// Return every cached block to the driver (all devices).
+void release_cached_device_blocks();
 
 struct KsgOutputs {
     float* mi = nullptr;     // device, indexed by pair order of the input list
