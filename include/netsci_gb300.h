@@ -54,6 +54,11 @@ const char* nsg_last_error(void);
 int nsg_version(void);
 /* Frees memory returned by the library (nsg_recover_single_shortest_path). */
 void nsg_free(void* p);
+/* Device memory the library has freed is kept in a per-device cache (at most
+ * 32 GiB per device) and reused by later plans; it is returned to the driver
+ * when an allocation of the library fails. This returns all of it now, for a
+ * caller about to allocate device memory of its own. */
+int nsg_release_cached_memory(void);
 
 /* ---- 1. CuArray handles (cuarray/include/cuarray.h:23-489) -------------- */
 typedef struct nsg_cuarray nsg_cuarray;

@@ -73,6 +73,7 @@ class NsgError(RuntimeError):
 _SIGNATURES = {
     "nsg_last_error": (c_char_p, []),
     "nsg_version": (c_int, []),
+    "nsg_release_cached_memory": (c_int, []),
     "nsg_free": (None, [c_void_p]),
     "nsg_cuarray_create": (c_int, [c_int, PP_void]),
     "nsg_cuarray_destroy": (c_int, [c_void_p]),

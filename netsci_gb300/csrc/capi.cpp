@@ -98,6 +98,10 @@ extern "C" {
 
 const char* nsg_last_error(void) { return g_last_error.c_str(); }
 int nsg_version(void) { return 100; }
+
+int nsg_release_cached_memory(void) {
+    return guarded([&] { nsg::release_cached_device_blocks(); });
+}
 void nsg_free(void* p) { delete[] static_cast<int*>(p); }
 
 // ---- CuArray ---------------------------------------------------------------

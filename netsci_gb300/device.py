@@ -158,6 +158,11 @@ class KsgPlan:
             pass
 
 
+def release_cached_memory() -> None:
+    """Return the device memory the library keeps for reuse to the driver."""
+    call("nsg_release_cached_memory")
+
+
 def set_ksg_shape(threads: int = 0, r: int = 0, frames: int = 0, variant: int = -1) -> None:
     """Force a KSG tile shape for later plans (threads=0: automatic)."""
     call("nsg_ksg_set_shape", int(threads), int(r), int(frames), int(variant))

@@ -392,3 +392,32 @@ def test_bootstrap_duplicates_and_real_ties(oracle_mod):
                 assert np.array_equal(mi.cpu().numpy(), expect), name
     finally:
         device.set_ksg_search(-1)
+
+
+def test_cached_device_memory_reused_and_released(oracle_mod):
+    """Plans built one after another reuse the blocks earlier plans freed;
+    nsg_release_cached_memory returns them to the driver, and plans built
+    afterwards still give the oracle's results."""
+    from netsci_gb300 import device, synthetic
+    N, m, k = 4, 1500, 6
+    X, _ = synthetic.protein_trajectory(N, m, seed=9)
+    Xd, mm = device.pack_trajectory(X, 3)
+    ab = synthetic.all_pairs(N)
+    expect = oracle_mod.pairs(X, m, 3, ab, k, gc=False, threads=8)
+    mi = torch.empty(len(ab), device="cuda")
+    torch.cuda.synchronize()
+
+    def run_once():
+        plan = device.KsgPlan(device.make_pairs(Xd, mm, ab), k, 3, mi=mi)
+        plan.run()
+        torch.cuda.synchronize()
+        plan.check()
+        plan.close()
+        assert np.array_equal(mi.cpu().numpy(), expect)
+
+    for _ in range(3):
+        run_once()
+    held = torch.cuda.mem_get_info()[0]
+    device.release_cached_memory()
+    assert torch.cuda.mem_get_info()[0] > held
+    run_once()
