@@ -30,7 +30,7 @@ namespace nsg {
 namespace {
 
 constexpr int kWarpsPerCta = 8;
-constexpr int kCtasPerSm = 2;
+constexpr int kCtasPerSm = 4;  // latency-bound: as many warps as 64 registers allow
 constexpr int kStack = 64;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -184,7 +184,7 @@ __device__ bool sort_prefix_warp(const float* key, int* idx, int n, int T, SortS
 }
 
 template <int D>
-__global__ void __launch_bounds__(kWarpsPerCta * 32) ksg_tie_kernel(KsgTieArgs A) {
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kCtasPerSm) ksg_tie_kernel(KsgTieArgs A) {
     __shared__ SortSegment s_stack[kWarpsPerCta][kStack];
     const int lane = threadIdx.x & 31;
     const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
