@@ -590,6 +590,7 @@ void KsgPlan::enqueue(cudaStream_t s) {
 struct KsgPlan::GridState {
     DeviceBuffer nodes, node_arena;       // GridNode[nnodes] and their buffers
     DeviceBuffer gps, pair_arena;         // GridPair per plan pair; pair grids of one batch
+    std::vector<int> batch_maxm;          // largest m of each batch
     DeviceBuffer wprefix;                 // per batch: npairs+1 prefix of ceil(m/32)
     std::vector<long long> wprefix_off;   // offset of each batch's prefix
     DeviceBuffer groups, gprefix;         // count groups and their item prefix, per batch
@@ -671,8 +672,9 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
     for (const Batch& b : batches_) {
         size_t off = 0;
         g->wprefix_off.push_back(static_cast<long long>(wpre.size()));
-        int acc = 0;
+        int acc = 0, maxm = 0;
         for (int p = b.pair0; p < b.pair0 + b.npairs; ++p) {
+            maxm = std::max(maxm, descs[p].m);
             wpre.push_back(acc);
             acc += (descs[p].m + 31) / 32;
             const int G = nodes[gps[p].a].G;
@@ -684,6 +686,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
             off += align16(static_cast<size_t>(2 * d_) * descs[p].m * sizeof(float));
         }
         wpre.push_back(acc);
+        g->batch_maxm.push_back(maxm);
         pair_arena = std::max(pair_arena, off);
     }
     g->pair_arena.reset(std::max<size_t>(pair_arena, 16));
@@ -745,7 +748,7 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         int* ctr = counters_.as<int>() + kCounters * bi;
         KsgPairDesc* bp = pairs_dev_.as<KsgPairDesc>() + b.pair0;
         GridPair* bg = g.gps.as<GridPair>() + b.pair0;
-        grid_launch_pairs(bp, bg, g.nodes.as<GridNode>(), b.npairs, d_, s);
+        grid_launch_pairs(bp, bg, g.nodes.as<GridNode>(), b.npairs, g.batch_maxm[bi], d_, s);
         GridArgs a{};
         a.pairs = bp;
         a.gp = bg;

@@ -221,6 +221,60 @@ __global__ void __launch_bounds__(kPrepThreads) grid_pair_kernel(const KsgPairDe
     build_query_order(s_cnt, G, gp.start, s_tmp1, s_tmp2);
 }
 
+// The same pair grid, written plane by plane through shared memory: each
+// frame's position is computed once, then every output plane (the original
+// indices and the 2d coordinates) is scattered into a shared-memory buffer
+// and written out with coalesced stores, instead of scattering 2d + 1 values
+// per frame across global memory. Dynamic shared memory: 8 * mpad bytes
+// (positions, then the plane buffer) with mpad >= m.
+template <int D>
+__global__ void __launch_bounds__(kPrepThreads) grid_pair_staged_kernel(const KsgPairDesc* pairs,
+                                                                       GridPair* gps,
+                                                                       const GridNode* nodes, int mpad) {
+    extern __shared__ int s_dyn[];
+    __shared__ int s_cnt[kGridMaxG * kGridMaxG];
+    __shared__ int s_start[kGridMaxG * kGridMaxG + 1];
+    __shared__ int s_tmp1[kGridMaxG * kGridMaxG], s_tmp2[kGridMaxG * kGridMaxG + 1];
+    int* s_pos = s_dyn;
+    int* s_buf = s_dyn + mpad;
+    const KsgPairDesc P = pairs[blockIdx.x];
+    const GridPair gp = gps[blockIdx.x];
+    const GridNode na = nodes[gp.a], nb = nodes[gp.b];
+    const int m = P.m, G = na.G, t = threadIdx.x;
+    for (int c = t; c < G * G; c += blockDim.x) s_cnt[c] = 0;
+    __syncthreads();
+    for (int j = t; j < m; j += blockDim.x) {
+        const int cell = (na.cell[j] / G) * G + nb.cell[j] / G;
+        s_pos[j] = cell;
+        atomicAdd(&s_cnt[cell], 1);
+    }
+    __syncthreads();
+    block_scan(s_cnt, s_start, G * G);
+    for (int c = t; c <= G * G; c += blockDim.x) gp.start[c] = s_start[c];
+    for (int c = t; c < G * G; c += blockDim.x) s_cnt[c] = 0;
+    __syncthreads();
+    for (int j = t; j < m; j += blockDim.x) {
+        const int cell = s_pos[j];
+        s_pos[j] = s_start[cell] + atomicAdd(&s_cnt[cell], 1);
+    }
+    __syncthreads();
+    for (int j = t; j < m; j += blockDim.x) s_buf[s_pos[j]] = j;
+    __syncthreads();
+    for (int q = t; q < m; q += blockDim.x) gp.perm[q] = s_buf[q];
+    float* fbuf = reinterpret_cast<float*>(s_buf);
+#pragma unroll 1
+    for (int c = 0; c < 2 * D; ++c) {
+        const float* src = c < D ? P.xa + static_cast<long long>(c) * P.ld : P.xb + static_cast<long long>(c - D) * P.ld;
+        __syncthreads();
+        for (int j = t; j < m; j += blockDim.x) fbuf[s_pos[j]] = __ldg(src + j);
+        __syncthreads();
+        float* dst = gp.sx + static_cast<long long>(c) * m;
+        for (int q = t; q < m; q += blockDim.x) dst[q] = fbuf[q];
+    }
+    __syncthreads();
+    build_query_order(s_cnt, G, gp.start, s_tmp1, s_tmp2);
+}
+
 // psi[n_x] + psi[n_y] per sample from the raw counts (self included), as
 // write_outputs does in the exhaustive kernel.
 __global__ void grid_combine_kernel(const KsgPairDesc* pairs, const int* cnt_a, const int* cnt_b,
@@ -309,13 +363,35 @@ void grid_launch_nodes(GridNode* nodes, int nnodes, int d, cudaStream_t st) {
     NSG_CUDA(cudaGetLastError());
 }
 
+namespace {
+
+// Largest dynamic shared memory the staged pair-grid kernel asks for.
+constexpr size_t kPairStagedSmem = size_t(160) << 10;
+
+template <int D>
+void launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs, int max_m,
+                  cudaStream_t st) {
+    const int mpad = (max_m + 3) & ~3;
+    const size_t smem = sizeof(int) * 2 * static_cast<size_t>(mpad);
+    if (smem <= kPairStagedSmem) {
+        // set on every launch: the attribute belongs to the current device
+        NSG_CUDA(cudaFuncSetAttribute(grid_pair_staged_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(kPairStagedSmem)));
+        grid_pair_staged_kernel<D><<<npairs, kPrepThreads, smem, st>>>(pairs, gps, nodes, mpad);
+    } else {
+        grid_pair_kernel<D><<<npairs, kPrepThreads, 0, st>>>(pairs, gps, nodes);
+    }
+}
+
+}  // namespace
+
 void grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
-                       int d, cudaStream_t st) {
+                       int max_m, int d, cudaStream_t st) {
     if (npairs <= 0) return;
     switch (d) {
-        case 1: grid_pair_kernel<1><<<npairs, kPrepThreads, 0, st>>>(pairs, gps, nodes); break;
-        case 2: grid_pair_kernel<2><<<npairs, kPrepThreads, 0, st>>>(pairs, gps, nodes); break;
-        case 3: grid_pair_kernel<3><<<npairs, kPrepThreads, 0, st>>>(pairs, gps, nodes); break;
+        case 1: launch_pairs<1>(pairs, gps, nodes, npairs, max_m, st); break;
+        case 2: launch_pairs<2>(pairs, gps, nodes, npairs, max_m, st); break;
+        case 3: launch_pairs<3>(pairs, gps, nodes, npairs, max_m, st); break;
         default: invalid("d must be 1, 2 or 3");
     }
     NSG_CUDA(cudaGetLastError());

@@ -109,8 +109,9 @@ int grid_cells_per_axis(int m);
 // Node grids (nodes: device array whose x, ld, m, G and buffers are set).
 void grid_launch_nodes(GridNode* nodes, int nnodes, int d, cudaStream_t st);
 // Pair grids of a batch (pairs, gps: device arrays of npairs).
+// max_m: the largest m of the pairs (sizes the shared-memory staging).
 void grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
-                       int d, cudaStream_t st);
+                       int max_m, int d, cudaStream_t st);
 void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st);
 void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st);
 void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a, const int* cnt_b,

@@ -405,6 +405,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
 
     // descriptors, pair-grid arena offsets, warp-block prefix
     long long samples = 0, wacc = 0;
+    int maxm = 0;
     size_t arena = 0;
     long long p = 0;
     std::vector<long long> slice_first(slices.size());
@@ -435,6 +436,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
             arena += align16(static_cast<size_t>(2 * d) * pr.m * sizeof(float));
             h_wpre_[p] = static_cast<int>(wacc);
             wacc += (pr.m + 31) / 32;
+            maxm = std::max(maxm, pr.m);
         }
     }
     h_wpre_[np] = static_cast<int>(wacc);
@@ -474,7 +476,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     NSG_CUDA(cudaMemsetAsync(d_counters_.get(), 0, sizeof(int) * 4, s));
     int* ctr = d_counters_.as<int>();
     KsgPairDesc* dp = d_pairs_.as<KsgPairDesc>();
-    grid_launch_pairs(dp, d_gpairs_.as<GridPair>(), d_gnodes_.as<GridNode>(), static_cast<int>(np), d, s);
+    grid_launch_pairs(dp, d_gpairs_.as<GridPair>(), d_gnodes_.as<GridNode>(), static_cast<int>(np), maxm, d, s);
     GridArgs a{};
     a.pairs = dp;
     a.gp = d_gpairs_.as<GridPair>();
