@@ -133,6 +133,35 @@ __device__ __forceinline__ void stage(float* tile, int* jt, const float* sx, lon
     }
 }
 
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Issue the copies of frames [base, base+n), n <= 64, into a half tile
+// (planes of stride kGridChunk) with their indices in jt; +inf past n.
+template <int NP>
+__device__ __forceinline__ void stage_async(float* tile, int* jt, const float* sx, long long stride,
+                                            const int* perm, int base, int n, int lane) {
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const int f = lane + 32 * t;
+        if (f < n) {
+#pragma unroll
+            for (int c = 0; c < NP; ++c) cp_async4(tile + c * kGridChunk + f, sx + c * stride + base + f);
+            cp_async4(jt + f, perm + base + f);
+        } else {
+#pragma unroll
+            for (int c = 0; c < NP; ++c) tile[c * kGridChunk + f] = inf_f();
+            jt[f] = -1;
+        }
+    }
+    cp_async_commit();
+}
+
 // Pass 1 over a staged chunk: frames' original indices in jt. The list holds
 // the KN nearest frames other than the query itself, with the flag `tied`
 // for a frame outside it at the k-th distance (ksgk::admit).
@@ -365,12 +394,26 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
                 }
             }
             scanned += hi - lo;
-            for (int base = lo; base < hi; base += kGridChunk) {
-                const int n = min(kGridChunk, hi - base);
+            if (hi > lo) {
+                // 64-frame halves of the tile, the next one loading while this one is scanned
+                const int nc = (hi - lo + 63) >> 6;
                 __syncwarp();
-                stage<2 * D, true>(tile, jt, gp.sx, st, gp.perm, base, n, lane);
-                __syncwarp();
-                pass1_chunk<D, KL>(tile, jt, n, qa, qb, bd, bj, self_seen, tied);
+                stage_async<2 * D>(tile, jt, gp.sx, st, gp.perm, lo, min(64, hi - lo), lane);
+                for (int ci = 0; ci < nc; ++ci) {
+                    const int half = ci & 1;
+                    if (ci + 1 < nc) {
+                        const int nb = lo + 64 * (ci + 1);
+                        stage_async<2 * D>(tile + 64 * (half ^ 1), jt + 64 * (half ^ 1), gp.sx, st, gp.perm, nb,
+                                           min(64, hi - nb), lane);
+                        cp_async_wait<1>();
+                    } else {
+                        cp_async_wait<0>();
+                    }
+                    __syncwarp();
+                    pass1_chunk<D, KL>(tile + 64 * half, jt + 64 * half, min(64, hi - lo - 64 * ci), qa, qb, bd,
+                                       bj, self_seen, tied);
+                    __syncwarp();
+                }
             }
         }
         if (A.evals && lane == 0) {
