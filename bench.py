@@ -60,7 +60,7 @@ N_NODES, M_FRAMES, DIM, K_NN = 2000, 10000, 3, 6
 # capture of a 256-pair step of this workload (profiles/ksg_grid_kernels_N2000_m10000.md:
 # pass 1 109.6 MB read + 13.5 MB written, counts 63.1 + 5.7 MB); the traffic
 # is per pair (each pair's grid copies and rows), so it scales with the pairs.
-GRID_DRAM_BYTES_PER_PAIR = (111.0 + 14.7 + 64.4 + 6.8) * 1e6 / 256
+GRID_DRAM_BYTES_PER_PAIR = (112.1 + 15.0 + 64.4 + 8.9) * 1e6 / 256
 SEED = 2000
 METRIC = "GC pairs/sec (batched persistent), N=2000 nodes, m=10000 frames"
 
