@@ -165,6 +165,12 @@ int g_forced_search = -1;
 // a few cells per axis prune little (measured: 0.91x at m = 300, 1.08x at
 // m = 1000, 1.28x at m = 2000, whole plans of 48-node trajectories).
 constexpr int kGridMinSamples = 1000;
+// Plans of a few pairs cannot fill the GPU and wait on launch and setup
+// latency, where the grid's three extra launches cost more: one pair took
+// 0.28 ms exhaustive against 0.33 ms on grids at m = 2000, and 0.90 against
+// 0.72 ms at m = 10000.
+constexpr int kGridFewPairs = 8;
+constexpr int kGridMinSamplesFew = 4000;
 // per batch: work-queue heads (two for the grid search), tie count, tie-kernel counter
 constexpr int kCounters = 4;
 }  // namespace
@@ -299,11 +305,12 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const 
     };
     std::map<RowKey, size_t> mapped;  // row -> offset (floats) of its copy
     size_t mapped_floats = 0;
-    double work = 0, work_large = 0;  // sum of m^2, and over pairs with m >= kGridMinSamples
+    double work = 0, work_large = 0;  // sum of m^2, and over pairs with m >= the grid's minimum
+    const int grid_min_m = npairs < kGridFewPairs ? kGridMinSamplesFew : kGridMinSamples;
     for (const auto& q : pairs_in) {
         const double w = static_cast<double>(q.m) * q.m;
         work += w;
-        if (q.m >= kGridMinSamples) work_large += w;
+        if (q.m >= grid_min_m) work_large += w;
         if (!q.fmap) continue;
         for (const float* x : {q.xa, q.xb}) {
             if (mapped.emplace(RowKey{x, q.fmap, q.m, q.ld}, mapped_floats).second) {
