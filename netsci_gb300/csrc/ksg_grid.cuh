@@ -133,6 +133,8 @@ __device__ __forceinline__ void stage(float* tile, int* jt, const float* sx, lon
     }
 }
 
+// 4-byte asynchronous global -> shared copies (cp.async), grouped per call
+// of stage_async and waited for with cp.async.wait_group.
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
     const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
@@ -142,7 +144,9 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // Issue the copies of frames [base, base+n), n <= 64, into a half tile
-// (planes of stride kGridChunk) with their indices in jt; +inf past n.
+// (planes of stride kGridChunk) with their indices in jt, as one group;
+// slots past n are set to +inf (index -1) directly. Frames are single floats
+// at arbitrary offsets, so the copies are 4 bytes each.
 template <int NP>
 __device__ __forceinline__ void stage_async(float* tile, int* jt, const float* sx, long long stride,
                                             const int* perm, int base, int n, int lane) {
