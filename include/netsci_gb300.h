@@ -255,7 +255,7 @@ int nsg_ksg_plan_evaluations(const nsg_ksg_plan* plan, unsigned long long* searc
  * nsg_ksg_pair_detail_device; mi, gc: device float[1] each, one nullable.
  * Synchronizes `stream`.                                                  */
 #define NSG_NOALLOC_MAX_SAMPLES 65536
-#define NSG_NOALLOC_SCRATCH_BYTES 9716480
+#define NSG_NOALLOC_SCRATCH_BYTES 9454336
 int nsg_ksg_pair_noalloc_device(const float* xa, const float* xb, int ld, int m, int k, int d,
                                 float* mi, float* gc, void* stream);
 

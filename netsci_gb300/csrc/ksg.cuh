@@ -36,7 +36,6 @@ struct KsgItem {
 struct KsgTie {
     int pair;             // index into the pair descriptor array
     int q;                // sample
-    float wk;             // its k-th (= (k+1)-th) joint distance
 };
 
 struct KsgCountArgs {

@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
             base = __shfl_sync(0xffffffffu, base, 0);
             if (tie) {
                 const int slot = base + __popc(tmask & ((1u << lane) - 1u));
-                if (slot < A.tie_cap) A.ties[slot] = KsgTie{A.pair_base + p, i, wk};
+                if (slot < A.tie_cap) A.ties[slot] = KsgTie{A.pair_base + p, i};
                 else atomicOr(A.fault, FAULT_TIE_OVERFLOW);
             }
         }

@@ -326,13 +326,13 @@ __device__ __forceinline__ void eps_and_ties(const KsgCountArgs& A, const KsgIte
 template <int R>
 __device__ __forceinline__ void report_ties(const KsgCountArgs& A, const KsgItem& w,
                                             const int (&qi)[R], const bool (&tie)[R],
-                                            const bool (&mixed)[R], const float (&wk)[R]) {
+                                            const bool (&mixed)[R]) {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         if (tie[r] && mixed[r]) {
             const int slot = atomicAdd(A.tie_count, 1);
             if (slot < A.tie_cap) {
-                A.ties[slot] = KsgTie{w.pair, qi[r], wk[r]};
+                A.ties[slot] = KsgTie{w.pair, qi[r]};
             } else {
                 atomicOr(A.fault, FAULT_TIE_OVERFLOW);
             }
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel(KsgCountArgs A) {
                                                  cb, wk, ra, rb, mixed);
             }
         }
-        report_ties<R>(A, w, qi, tie, mixed, wk);
+        report_ties<R>(A, w, qi, tie, mixed);
         write_outputs<R>(A, w, P, qi, wk, ea, eb, ca, cb);
     }
 }
@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(NT) ksg_count_kernel_tma(KsgCountArgs A) {
                 else inflight0 += 1;
             }
         }
-        report_ties<R>(A, w, qi, tie, mixed, wk);
+        report_ties<R>(A, w, qi, tie, mixed);
         write_outputs<R>(A, w, P, qi, wk, ea, eb, ca, cb);
     }
 }
