@@ -471,8 +471,10 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const 
             dd.out = src;
             dd.pad = 0;
             dd.scratch = per_sample ? prefix[src] : used;
-            for (int q0 = 0; q0 < q.m; q0 += qc) {
-                items.push_back({pos, q0, std::min(q.m, q0 + qc), 0});
+            if (!search_) {  // the exhaustive kernel's work queue (the grid kernels index blocks)
+                for (int q0 = 0; q0 < q.m; q0 += qc) {
+                    items.push_back({pos, q0, std::min(q.m, q0 + qc), 0});
+                }
             }
             used += q.m;
             ++b.npairs;
@@ -489,9 +491,11 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const 
         pairs_dev_.reset(descs.size() * sizeof(KsgPairDesc));
         NSG_CUDA(cudaMemcpy(pairs_dev_.get(), descs.data(), descs.size() * sizeof(KsgPairDesc),
                             cudaMemcpyHostToDevice));
-        items_dev_.reset(items.size() * sizeof(KsgItem));
-        NSG_CUDA(cudaMemcpy(items_dev_.get(), items.data(), items.size() * sizeof(KsgItem),
-                            cudaMemcpyHostToDevice));
+        if (!items.empty()) {
+            items_dev_.reset(items.size() * sizeof(KsgItem));
+            NSG_CUDA(cudaMemcpy(items_dev_.get(), items.data(), items.size() * sizeof(KsgItem),
+                                cudaMemcpyHostToDevice));
+        }
         scratch_.reset(static_cast<size_t>(scratch_need) * sizeof(float));
         // per batch: work-queue head, tie count, tie-kernel work counter
         counters_.reset(kCounters * batches_.size() * sizeof(int));
