@@ -52,24 +52,25 @@ namespace nsg {
 namespace ksgk {
 
 // Insert (v, j) into the ascending list (bd, bj), dropping its last entry;
-// the caller has checked v < bd[KMAX-1]. Branch-free: place at the end,
-// then one compare-and-swap per slot towards the front. Sentinel slots
-// (-inf) never move.
+// the caller has checked v < bd[KMAX-1]. Branch-free: every slot compares
+// with v once; a slot holding a larger value takes its left neighbour, or v
+// where that neighbour is not larger. v lands behind entries equal to it.
+// Sentinel slots (-inf) never move.
 template <int KMAX>
 __device__ __forceinline__ void list_insert(float (&bd)[KMAX], int (&bj)[KMAX], float v, int j) {
-    bd[KMAX - 1] = v;
-    bj[KMAX - 1] = j;
+    bool gt[KMAX];
+#pragma unroll
+    for (int s = 0; s < KMAX; ++s) gt[s] = v < bd[s];
 #pragma unroll
     for (int s = KMAX - 1; s > 0; --s) {
-        const bool sw = bd[s] < bd[s - 1];
-        const float lo = sw ? bd[s] : bd[s - 1];
-        const float hi = sw ? bd[s - 1] : bd[s];
-        const int jl = sw ? bj[s] : bj[s - 1];
-        const int jh = sw ? bj[s - 1] : bj[s];
-        bd[s - 1] = lo;
-        bd[s] = hi;
-        bj[s - 1] = jl;
-        bj[s] = jh;
+        if (gt[s]) {
+            bd[s] = gt[s - 1] ? bd[s - 1] : v;
+            bj[s] = gt[s - 1] ? bj[s - 1] : j;
+        }
+    }
+    if (gt[0]) {
+        bd[0] = v;
+        bj[0] = j;
     }
 }
 
