@@ -607,6 +607,7 @@ struct KsgPlan::GridState {
     DeviceBuffer groups, gprefix;         // count groups and their item prefix, per batch
     std::vector<long long> group_off, gprefix_off;
     std::vector<int> ngroups;
+    DeviceBuffer corder;                  // count-query order: ngroups x largest m of a batch
     DeviceBuffer eps_a, eps_b, cnt_a, cnt_b;
     DeviceBuffer evals;                   // 2 counters per run (search, counts)
     int nnodes = 0;
@@ -724,6 +725,11 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
             gpre.push_back(acc);
             g->ngroups.push_back(static_cast<int>(groups.size() - first));
         }
+        size_t corder = 0;
+        for (size_t bi = 0; bi < batches_.size(); ++bi) {
+            corder = std::max(corder, static_cast<size_t>(g->ngroups[bi]) * g->batch_maxm[bi]);
+        }
+        g->corder.reset(std::max<size_t>(1, corder) * sizeof(int));
         g->groups.reset(std::max<size_t>(1, groups.size()) * sizeof(CountGroup));
         if (!groups.empty()) {
             NSG_CUDA(cudaMemcpy(g->groups.get(), groups.data(), groups.size() * sizeof(CountGroup),
@@ -784,6 +790,8 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         a.eps_x = out_.eps_x;
         a.eps_y = out_.eps_y;
         a.kdist = out_.kdist;
+        a.corder = g.corder.as<int>();
+        a.corder_ld = g.batch_maxm[bi];
         if (timing_) record_event(events_[2 * bi], s);
         grid_launch_search(a, d_, kmax_, g.search_grid, s);
         a.counter = ctr + 1;

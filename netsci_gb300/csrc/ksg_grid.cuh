@@ -493,12 +493,13 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
 
 // ---- pass 2: marginal counts on a node grid -------------------------------------
 // A work item is a count group (up to kCountGroup pairs that count the same
-// node's variable) and a block of kCountQueries queries consecutive in that
-// node grid's query order, two lanes per query. The warp visits the union of the queries' boxes for the
+// node's variable) and a block of kCountQueries queries consecutive in the
+// group's count order (A.corder, else the node grid's query order), two
+// lanes per query. The warp visits the union of the queries' boxes for the
 // largest of the pairs' eps, row by row over the columns of the boxes that
 // hold the row, and counts every pair from one distance per frame.
 template <int D>
-__global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArgs A) {
+__global__ void __launch_bounds__(32 * kGridWarps, 4) ksg_grid_count_kernel(GridArgs A) {
     using namespace gridk;
     __shared__ __align__(16) float s_tile[kGridWarps][D * kGridChunk];
     const int lane = threadIdx.x & 31;
@@ -519,20 +520,20 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
         const int m = nd.m, G = nd.G;
         const long long st = m;
         const int half = lane & 1;  // two lanes per query
-        const int qi = blk * kCountQueries + (lane >> 1);  // query rank in the node grid's query order
+        const int qi = blk * kCountQueries + (lane >> 1);  // query rank in the group's count order
         const bool valid = qi < m;
-        const int r = valid ? query_position(nd.start, G, qi) : 0;
+        const int r = !valid ? 0
+                      : A.corder ? __ldg(A.corder + static_cast<long long>(gi) * A.corder_ld + qi)
+                                 : query_position(nd.start, G, qi);
         const int i = valid ? __ldg(nd.perm + r) : 0;
         float q[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) q[c] = valid ? __ldg(nd.sx + c * st + r) : 0.f;
         float e[kCountGroup];
-        long long o[kCountGroup];
         float emax = -inf_f();
 #pragma unroll
         for (int p = 0; p < kCountGroup; ++p) {
-            o[p] = p < grp.npairs ? A.pairs[grp.pairs[p]].scratch + i : 0;
-            e[p] = (valid && p < grp.npairs) ? __ldg(eps + o[p]) : -inf_f();
+            e[p] = (valid && p < grp.npairs) ? __ldg(eps + A.pairs[grp.pairs[p]].scratch + i) : -inf_f();
             emax = fmaxf(emax, e[p]);
         }
         const float q1 = q[nd.c1];
@@ -571,7 +572,7 @@ __global__ void __launch_bounds__(32 * kGridWarps) ksg_grid_count_kernel(GridArg
         if (valid && half == 0) {
 #pragma unroll
             for (int p = 0; p < kCountGroup; ++p)
-                if (p < grp.npairs) out[o[p]] = cnt[p];
+                if (p < grp.npairs) out[A.pairs[grp.pairs[p]].scratch + i] = cnt[p];
         }
         if (A.evals && lane == 0) {
             atomicAdd(A.evals + 1, static_cast<unsigned long long>(scanned) *

@@ -88,7 +88,19 @@ struct GridArgs {
     float* eps_x;
     float* eps_y;
     float* kdist;
+    // Count-query order per group (row gi at corder + gi * corder_ld, at
+    // least m entries; nullptr: the node grids' own query order). Filled by
+    // grid_launch_counts before the counts.
+    int* corder;
+    int corder_ld;
 };
+
+// Count-query order: the node grid's cells in kOrderBlock x kOrderBlock
+// blocks, blocks in Z order, and within a block the queries by the largest
+// eps of the group's pairs. Ordered when m <= kOrderMaxM (the eps of one
+// group fit in shared memory).
+constexpr int kOrderBlock = 4;
+constexpr int kOrderMaxM = 40960;
 
 // A frame-mapped row copied out for the cell-grid search:
 // out[c*ld_out + s] = x[c*ld + fmap[s]] for s < m, +inf up to ld_out.

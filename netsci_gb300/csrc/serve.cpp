@@ -470,6 +470,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         gpre[gi + 1] = gpre[gi] + (h_pairs_[groups[gi].pairs[0]].m + kCountQueries - 1) / kCountQueries;
     }
+    ensure(d_corder_, sizeof(int) * std::max<size_t>(1, groups.size() * static_cast<size_t>(maxm)));
     NSG_CUDA(cudaMemcpyAsync(d_groups_.get(), groups.data(), sizeof(CountGroup) * groups.size(),
                              cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemcpyAsync(d_gpre_.get(), gpre.data(), sizeof(int) * gpre.size(), cudaMemcpyHostToDevice, s));
@@ -497,6 +498,8 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     a.eps_b = d_eps_b_.as<float>();
     a.cnt_a = d_cnt_a_.as<int>();
     a.cnt_b = d_cnt_b_.as<int>();
+    a.corder = d_corder_.as<int>();
+    a.corder_ld = maxm;
     const int sms = sm_count();
     grid_launch_search(a, d, kmax, sms * grid_search_ctas_per_sm(d, kmax), s);
     a.counter = ctr + 1;

@@ -104,6 +104,7 @@ private:
     // and per-tick pair grids and scratch, grown on demand
     DeviceBuffer d_gnodes_, d_gpairs_, d_wpre_, d_garena_, d_eps_a_, d_eps_b_, d_cnt_a_, d_cnt_b_;
     DeviceBuffer d_groups_, d_gpre_;
+    DeviceBuffer d_corder_;  // count-query order: groups x largest m of the tick
     GridPair* h_gpairs_ = nullptr;
     int* h_wpre_ = nullptr;
     int next_node_slot_ = 0;
