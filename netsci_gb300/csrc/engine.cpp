@@ -614,10 +614,6 @@ struct KsgPlan::GridState {
     int search_grid = 0, count_grid = 0;
 };
 
-namespace {
-size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
-}  // namespace
-
 void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
     auto g = std::make_shared<GridState>();
     // nodes: one per distinct (row, m, ld)
@@ -643,13 +639,9 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
         n.x = x;
         n.ld = ld;
         n.m = m;
-        n.G = grid_cells_per_axis(m);
         nodes.push_back(n);
         node_off.push_back(arena);
-        arena += align16(2 * kGridMaxG * sizeof(float)) + grid_index_bytes(n.G) +
-                 align16(static_cast<size_t>(m) * sizeof(unsigned short)) +
-                 align16(static_cast<size_t>(m) * sizeof(int)) +
-                 align16(static_cast<size_t>(d_) * m * sizeof(float));
+        arena += grid_node_bytes(m, d_);
         return id;
     };
     std::vector<GridPair> gps(descs.size());
@@ -661,18 +653,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
     g->node_arena.reset(std::max<size_t>(arena, 16));
     unsigned char* base = g->node_arena.as<unsigned char>();
     for (size_t i = 0; i < nodes.size(); ++i) {
-        GridNode& n = nodes[i];
-        unsigned char* q = base + node_off[i];
-        n.e1 = reinterpret_cast<float*>(q);
-        n.e2 = n.e1 + kGridMaxG;
-        q += align16(2 * kGridMaxG * sizeof(float));
-        n.start = reinterpret_cast<int*>(q);
-        q += grid_index_bytes(n.G);
-        n.cell = reinterpret_cast<unsigned short*>(q);
-        q += align16(static_cast<size_t>(n.m) * sizeof(unsigned short));
-        n.perm = reinterpret_cast<int*>(q);
-        q += align16(static_cast<size_t>(n.m) * sizeof(int));
-        n.sx = reinterpret_cast<float*>(q);
+        nodes[i] = grid_node_at(base + node_off[i], nodes[i].x, nodes[i].ld, nodes[i].m);
     }
     g->nodes.reset(nodes.size() * sizeof(GridNode));
     NSG_CUDA(cudaMemcpy(g->nodes.get(), nodes.data(), nodes.size() * sizeof(GridNode),
@@ -689,25 +670,14 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
             maxm = std::max(maxm, descs[p].m);
             wpre.push_back(acc);
             acc += (descs[p].m + 31) / 32;
-            const int G = nodes[gps[p].a].G;
-            gps[p].start = reinterpret_cast<int*>(off);
-            off += grid_index_bytes(G);
-            gps[p].perm = reinterpret_cast<int*>(off);
-            off += align16(static_cast<size_t>(descs[p].m) * sizeof(int));
-            gps[p].sx = reinterpret_cast<float*>(off);
-            off += align16(static_cast<size_t>(2 * d_) * descs[p].m * sizeof(float));
+            off = grid_pair_place(gps[p], off, descs[p].m, d_);
         }
         wpre.push_back(acc);
         g->batch_maxm.push_back(maxm);
         pair_arena = std::max(pair_arena, off);
     }
     g->pair_arena.reset(std::max<size_t>(pair_arena, 16));
-    const uintptr_t pbase = reinterpret_cast<uintptr_t>(g->pair_arena.get());
-    for (auto& gp : gps) {
-        gp.start = reinterpret_cast<int*>(pbase + reinterpret_cast<uintptr_t>(gp.start));
-        gp.perm = reinterpret_cast<int*>(pbase + reinterpret_cast<uintptr_t>(gp.perm));
-        gp.sx = reinterpret_cast<float*>(pbase + reinterpret_cast<uintptr_t>(gp.sx));
-    }
+    for (auto& gp : gps) grid_pair_rebase(gp, g->pair_arena.get());
     // count groups: pairs of a batch that count the same node's variable
     {
         std::vector<CountGroup> groups;
@@ -765,8 +735,9 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         int* ctr = counters_.as<int>() + kCounters * bi;
         KsgPairDesc* bp = pairs_dev_.as<KsgPairDesc>() + b.pair0;
         GridPair* bg = g.gps.as<GridPair>() + b.pair0;
-        grid_launch_pairs(bp, bg, g.nodes.as<GridNode>(), b.npairs, g.batch_maxm[bi], d_, s);
+        const int search_order = grid_launch_pairs(bp, bg, g.nodes.as<GridNode>(), b.npairs, g.batch_maxm[bi], d_, s);
         GridArgs a{};
+        a.search_order = search_order;
         a.pairs = bp;
         a.gp = bg;
         a.nodes = g.nodes.as<GridNode>();

@@ -182,6 +182,43 @@ __global__ void __launch_bounds__(kPrepThreads) grid_node_kernel(GridNode* nodes
     build_query_order(s_cnt, G, nd.start, s_tmp1, s_tmp2);
 }
 
+// One CTA per node, after grid_node_kernel: the scale estimate of every
+// frame (GridNode::est), from the frames of the 3 x 3 cells around its own.
+// Consecutive threads take consecutive positions, mostly of one cell, so
+// they read the same neighbour frames.
+template <int D>
+__global__ void __launch_bounds__(kPrepThreads) grid_node_est_kernel(const GridNode* nodes) {
+    const GridNode nd = nodes[blockIdx.x];
+    const int m = nd.m, G = nd.G;
+    const long long st = m;
+    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
+        const int j = __ldg(nd.perm + pos);
+        const int c = __ldg(nd.cell + j);
+        const int row = c / G, col = c - (c / G) * G;
+        float q[D];
+#pragma unroll
+        for (int cc = 0; cc < D; ++cc) q[cc] = __ldg(nd.sx + cc * st + pos);
+        float bd[kEstRank];
+        int bj[kEstRank];
+#pragma unroll
+        for (int s = 0; s < kEstRank; ++s) {
+            bd[s] = __int_as_float(0x7f800000);
+            bj[s] = -1;
+        }
+        const int c0 = max(col - 1, 0), c1 = min(col + 1, G - 1);
+        for (int r = max(row - 1, 0); r <= min(row + 1, G - 1); ++r) {
+            const int lo = __ldg(nd.start + r * G + c0), hi = __ldg(nd.start + r * G + c1 + 1);
+            for (int f = lo; f < hi; ++f) {
+                float dm = 0.f;
+#pragma unroll
+                for (int cc = 0; cc < D; ++cc) dm = fmaxf(dm, fabsf(q[cc] - __ldg(nd.sx + cc * st + f)));
+                if (f != pos && dm < bd[kEstRank - 1]) ksgk::list_insert<kEstRank>(bd, bj, dm, f);
+            }
+        }
+        nd.est[j] = bd[kEstRank - 1];
+    }
+}
+
 // One CTA per pair of the batch: cells over (bin of a on its c1, bin of b on
 // its c1), counting sort, both nodes' coordinates copied in that order.
 template <int D>
@@ -290,11 +327,11 @@ __global__ void grid_combine_kernel(const KsgPairDesc* pairs, const int* cnt_a, 
     }
 }
 
-// Count-query order of one count group per CTA (see kOrderBlock). The queries
-// a warp counts together then sit in one block of cells with boxes of
-// similar size, so the union of their boxes is smaller than in the node
-// grid's Z order of cells (by about a sixth at m = 10000). Any order gives
-// the same counts; this one only shortens the scans.
+// Block orders of queries (see kOrderBlock). A warp's queries then sit in
+// one block of cells with boxes of similar size, so the union of their boxes
+// is smaller than in a grid's Z order of cells (by about a sixth for the
+// counts at m = 10000). Any order gives the same results; these only shorten
+// the scans.
 constexpr int kOrderThreads = 256;
 constexpr int kOrderBlocks = (kGridMaxG + kOrderBlock - 1) / kOrderBlock;  // per axis
 static_assert(kOrderBlocks <= 8, "block Z codes use three bits per axis");
@@ -306,26 +343,19 @@ __device__ __forceinline__ int block_zcode(int bx, int by) {
     return z;
 }
 
-__global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArgs A) {
-    extern __shared__ unsigned s_key[];  // [m] sort key per storage position
+// Sort key of a box size >= 0: its bits order as the values; NaN last.
+__device__ __forceinline__ unsigned order_key(float e) { return isnan(e) ? 0xffffffffu : __float_as_uint(e); }
+
+// Writes out[rank] = pos in the block order for every storage position pos
+// of a grid of G x G cells (cell index `start`), with the keys in s_key[pos]
+// and cell_of(pos, row, col) giving each position's cell. Called by the
+// whole CTA after it has written s_key. Keys with the position as tie-break
+// form a strict total order, so the ranks are always a permutation of [0, m).
+template <class CellOf>
+__device__ void write_block_order(const unsigned* s_key, const int* start, int G, int m, CellOf cell_of,
+                                  int* out) {
     __shared__ int s_boff[kOrderBlocks * kOrderBlocks];
-    const CountGroup grp = A.groups[blockIdx.x];
-    const GridNode nd = A.nodes[grp.node];
-    const float* eps = grp.side ? A.eps_b : A.eps_a;
-    const int m = nd.m, G = nd.G, nb = (G + kOrderBlock - 1) / kOrderBlock;
-    long long o[kCountGroup];
-#pragma unroll
-    for (int p = 0; p < kCountGroup; ++p) o[p] = A.pairs[grp.pairs[p]].scratch;  // unused slots repeat pairs[0]
-    // key: the largest eps of the group's pairs as its bits (eps >= 0, so
-    // they order as the values; NaN last), with the position breaking ties,
-    // a strict total order, so the ranks within a block are a permutation
-    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
-        const int j = __ldg(nd.perm + pos);
-        float e = __ldg(eps + o[0] + j);
-#pragma unroll
-        for (int p = 1; p < kCountGroup; ++p) e = fmaxf(e, __ldg(eps + o[p] + j));
-        s_key[pos] = isnan(e) ? 0xffffffffu : __float_as_uint(e);
-    }
+    const int nb = (G + kOrderBlock - 1) / kOrderBlock;
     // frames per block, then their exclusive prefix in Z order of the blocks
     if (threadIdx.x < kOrderBlocks * kOrderBlocks) {
         const int z = threadIdx.x;
@@ -339,7 +369,7 @@ __global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArg
         if (bx < nb && by < nb) {
             const int c0 = by * kOrderBlock, c1 = min(c0 + kOrderBlock, G);
             for (int r = bx * kOrderBlock; r < min((bx + 1) * kOrderBlock, G); ++r) {
-                n += __ldg(nd.start + r * G + c1) - __ldg(nd.start + r * G + c0);
+                n += __ldg(start + r * G + c1) - __ldg(start + r * G + c0);
             }
         }
         s_boff[z] = n;
@@ -354,16 +384,15 @@ __global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArg
         }
     }
     __syncthreads();
-    int* out = A.corder + static_cast<long long>(blockIdx.x) * A.corder_ld;
     for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
-        const int c = __ldg(nd.cell + __ldg(nd.perm + pos));
-        const int row = c / G, col = c - (c / G) * G;
+        int row, col;
+        cell_of(pos, row, col);
         const int bx = row / kOrderBlock, by = col / kOrderBlock;
         const unsigned key = s_key[pos];
         const int c0 = by * kOrderBlock, c1 = min(c0 + kOrderBlock, G);
         int rank = 0;
         for (int r = bx * kOrderBlock; r < min((bx + 1) * kOrderBlock, G); ++r) {
-            const int lo = __ldg(nd.start + r * G + c0), hi = __ldg(nd.start + r * G + c1);
+            const int lo = __ldg(start + r * G + c0), hi = __ldg(start + r * G + c1);
             for (int q = lo; q < hi; ++q) {
                 const unsigned kq = s_key[q];
                 rank += (kq < key || (kq == key && q < pos)) ? 1 : 0;
@@ -371,6 +400,54 @@ __global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArg
         }
         out[s_boff[block_zcode(bx, by)] + rank] = pos;
     }
+}
+
+// Count order of one count group per CTA: key = the largest eps of the
+// group's pairs. Dynamic shared memory: m keys.
+__global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArgs A) {
+    extern __shared__ unsigned s_key[];
+    const CountGroup grp = A.groups[blockIdx.x];
+    const GridNode nd = A.nodes[grp.node];
+    const float* eps = grp.side ? A.eps_b : A.eps_a;
+    const int m = nd.m, G = nd.G;
+    long long o[kCountGroup];
+#pragma unroll
+    for (int p = 0; p < kCountGroup; ++p) o[p] = A.pairs[grp.pairs[p]].scratch;  // unused slots repeat pairs[0]
+    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
+        const int j = __ldg(nd.perm + pos);
+        float e = __ldg(eps + o[0] + j);
+#pragma unroll
+        for (int p = 1; p < kCountGroup; ++p) e = fmaxf(e, __ldg(eps + o[p] + j));
+        s_key[pos] = order_key(e);
+    }
+    const auto cell_of = [&](int pos, int& row, int& col) {
+        const int c = __ldg(nd.cell + __ldg(nd.perm + pos));
+        row = c / G;
+        col = c - row * G;
+    };
+    write_block_order(s_key, nd.start, G, m, cell_of, A.corder + static_cast<long long>(blockIdx.x) * A.corder_ld);
+}
+
+// Search order of one pair per CTA: key = the larger of the two nodes' scale
+// estimates, which follows the k-th joint distance closely enough to group
+// queries with similar boxes. Dynamic shared memory: m keys.
+__global__ void __launch_bounds__(kOrderThreads) grid_pair_order_kernel(const KsgPairDesc* pairs,
+                                                                       const GridPair* gps,
+                                                                       const GridNode* nodes) {
+    extern __shared__ unsigned s_key[];
+    const GridPair gp = gps[blockIdx.x];
+    const GridNode na = nodes[gp.a], nb = nodes[gp.b];
+    const int m = pairs[blockIdx.x].m, G = na.G;
+    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
+        const int j = __ldg(gp.perm + pos);
+        s_key[pos] = order_key(fmaxf(__ldg(na.est + j), __ldg(nb.est + j)));
+    }
+    const auto cell_of = [&](int pos, int& row, int& col) {
+        const int j = __ldg(gp.perm + pos);
+        row = __ldg(na.cell + j) / G;
+        col = __ldg(nb.cell + j) / G;
+    };
+    write_block_order(s_key, gp.start, G, m, cell_of, gp.qpos);
 }
 
 // One CTA per row.
@@ -438,12 +515,74 @@ int grid_cells_per_axis(int m) {
 void grid_launch_nodes(GridNode* nodes, int nnodes, int d, cudaStream_t st) {
     if (nnodes <= 0) return;
     switch (d) {
-        case 1: grid_node_kernel<1><<<nnodes, kPrepThreads, 0, st>>>(nodes); break;
-        case 2: grid_node_kernel<2><<<nnodes, kPrepThreads, 0, st>>>(nodes); break;
-        case 3: grid_node_kernel<3><<<nnodes, kPrepThreads, 0, st>>>(nodes); break;
+        case 1:
+            grid_node_kernel<1><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            grid_node_est_kernel<1><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            break;
+        case 2:
+            grid_node_kernel<2><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            grid_node_est_kernel<2><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            break;
+        case 3:
+            grid_node_kernel<3><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            grid_node_est_kernel<3><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            break;
         default: invalid("d must be 1, 2 or 3");
     }
     NSG_CUDA(cudaGetLastError());
+}
+
+size_t grid_node_bytes(int m, int d) {
+    auto a16 = [](size_t b) { return (b + 15) & ~size_t(15); };
+    const size_t mm = static_cast<size_t>(m);
+    return a16(2 * kGridMaxG * sizeof(float)) + grid_index_bytes(grid_cells_per_axis(m)) +
+           a16(mm * sizeof(unsigned short)) + a16(mm * sizeof(int)) + a16(mm * sizeof(float)) +
+           a16(static_cast<size_t>(d) * mm * sizeof(float));
+}
+
+GridNode grid_node_at(unsigned char* base, const float* x, int ld, int m) {
+    auto a16 = [](size_t b) { return (b + 15) & ~size_t(15); };
+    const size_t mm = static_cast<size_t>(m);
+    GridNode n{};
+    n.x = x;
+    n.ld = ld;
+    n.m = m;
+    n.G = grid_cells_per_axis(m);
+    n.e1 = reinterpret_cast<float*>(base);
+    n.e2 = n.e1 + kGridMaxG;
+    base += a16(2 * kGridMaxG * sizeof(float));
+    n.start = reinterpret_cast<int*>(base);
+    base += grid_index_bytes(n.G);
+    n.cell = reinterpret_cast<unsigned short*>(base);
+    base += a16(mm * sizeof(unsigned short));
+    n.perm = reinterpret_cast<int*>(base);
+    base += a16(mm * sizeof(int));
+    n.est = reinterpret_cast<float*>(base);
+    base += a16(mm * sizeof(float));
+    n.sx = reinterpret_cast<float*>(base);
+    return n;
+}
+
+size_t grid_pair_place(GridPair& g, size_t off, int m, int d) {
+    auto a16 = [](size_t b) { return (b + 15) & ~size_t(15); };
+    const size_t mm = static_cast<size_t>(m);
+    g.start = reinterpret_cast<int*>(off);
+    off += grid_index_bytes(grid_cells_per_axis(m));
+    g.perm = reinterpret_cast<int*>(off);
+    off += a16(mm * sizeof(int));
+    g.qpos = reinterpret_cast<int*>(off);
+    off += a16(mm * sizeof(int));
+    g.sx = reinterpret_cast<float*>(off);
+    off += a16(static_cast<size_t>(2 * d) * mm * sizeof(float));
+    return off;
+}
+
+void grid_pair_rebase(GridPair& g, const void* base) {
+    const uintptr_t b = reinterpret_cast<uintptr_t>(base);
+    g.start = reinterpret_cast<int*>(b + reinterpret_cast<uintptr_t>(g.start));
+    g.perm = reinterpret_cast<int*>(b + reinterpret_cast<uintptr_t>(g.perm));
+    g.qpos = reinterpret_cast<int*>(b + reinterpret_cast<uintptr_t>(g.qpos));
+    g.sx = reinterpret_cast<float*>(b + reinterpret_cast<uintptr_t>(g.sx));
 }
 
 namespace {
@@ -468,9 +607,9 @@ void launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes
 
 }  // namespace
 
-void grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
-                       int max_m, int d, cudaStream_t st) {
-    if (npairs <= 0) return;
+int grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
+                      int max_m, int d, cudaStream_t st) {
+    if (npairs <= 0) return 0;
     switch (d) {
         case 1: launch_pairs<1>(pairs, gps, nodes, npairs, max_m, st); break;
         case 2: launch_pairs<2>(pairs, gps, nodes, npairs, max_m, st); break;
@@ -478,6 +617,14 @@ void grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* 
         default: invalid("d must be 1, 2 or 3");
     }
     NSG_CUDA(cudaGetLastError());
+    if (max_m > kOrderMaxM) return 0;
+    // set on every launch: the attribute belongs to the current device
+    NSG_CUDA(cudaFuncSetAttribute(grid_pair_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(sizeof(unsigned) * kOrderMaxM)));
+    grid_pair_order_kernel<<<npairs, kOrderThreads, sizeof(unsigned) * static_cast<size_t>(max_m), st>>>(
+        pairs, gps, nodes);
+    NSG_CUDA(cudaGetLastError());
+    return 1;
 }
 
 void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st) {

@@ -286,9 +286,9 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
         const GridNode nb = A.nodes[gp.b];
         const int m = P->m, G = na.G;
         const long long st = m;
-        const int qi = blk * 32 + lane;  // query rank in the grid's query order
+        const int qi = blk * 32 + lane;  // query rank in the pair's search order
         const bool valid = qi < m;
-        const int r = valid ? query_position(gp.start, G, qi) : 0;
+        const int r = !valid ? 0 : A.search_order ? __ldg(gp.qpos + qi) : query_position(gp.start, G, qi);
         const int i = valid ? __ldg(gp.perm + r) : 0;
         float qa[D], qb[D];
 #pragma unroll

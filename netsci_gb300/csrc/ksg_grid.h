@@ -39,7 +39,13 @@ struct GridNode {
     int* perm;             // [m] frames in cell order
     int* start;            // cell index (grid_index_bytes(G)), see above
     float* sx;             // [d][m] coordinates in cell order (plane stride m)
+    // [m] local scale of frame j: the distance to its kEstRank-th nearest
+    // frame among those of the 3 x 3 cells around its own (+inf if fewer)
+    float* est;
 };
+
+// Neighbour rank of the node scale estimate (GridNode::est).
+constexpr int kEstRank = 6;
 
 // Pair grid of one pair of a batch (device descriptor).
 struct GridPair {
@@ -47,6 +53,7 @@ struct GridPair {
     int* perm;             // [m] frames in pair-cell order
     int* start;            // cell index (grid_index_bytes(G)), see above
     float* sx;             // [2d][m] coordinates of a then b in that order
+    int* qpos;             // [m] search order: position of the query of each rank
 };
 
 // Pairs of a batch that count the same variable (node grid): their counts
@@ -93,12 +100,17 @@ struct GridArgs {
     // grid_launch_counts before the counts.
     int* corder;
     int corder_ld;
+    // 1: pass 1 takes its queries in the pairs' search order (GridPair::qpos,
+    // built by grid_launch_pairs); 0: in the grids' Z order of cells
+    int search_order;
 };
 
-// Count-query order: the node grid's cells in kOrderBlock x kOrderBlock
-// blocks, blocks in Z order, and within a block the queries by the largest
-// eps of the group's pairs. Ordered when m <= kOrderMaxM (the eps of one
-// group fit in shared memory).
+// Block orders of queries: a grid's cells in kOrderBlock x kOrderBlock
+// blocks, blocks in Z order, and within a block the queries by a key of
+// their box size, so that a warp's queries share a block and have boxes of
+// similar size. Counts: the largest eps of the group's pairs. Search: the
+// larger of the two nodes' scale estimates. Built when m <= kOrderMaxM (the
+// keys of one grid fit in shared memory).
 constexpr int kOrderBlock = 4;
 constexpr int kOrderMaxM = 40960;
 
@@ -118,12 +130,21 @@ void append_count_groups(const GridPair* gps, int npairs, std::vector<CountGroup
 
 // Cells per axis for m samples (about ten frames per cell, at most kGridMaxG).
 int grid_cells_per_axis(int m);
+// Bytes of one node grid's buffers, and its descriptor with the buffers at
+// `base` (16-byte aligned) for row x (stride ld) of m samples.
+size_t grid_node_bytes(int m, int d);
+GridNode grid_node_at(unsigned char* base, const float* x, int ld, int m);
+// Places a pair grid's buffers at byte offset `off` of a batch arena
+// (pointers hold offsets until grid_pair_rebase) and returns the end offset.
+size_t grid_pair_place(GridPair& g, size_t off, int m, int d);
+void grid_pair_rebase(GridPair& g, const void* base);
 // Node grids (nodes: device array whose x, ld, m, G and buffers are set).
 void grid_launch_nodes(GridNode* nodes, int nnodes, int d, cudaStream_t st);
-// Pair grids of a batch (pairs, gps: device arrays of npairs).
-// max_m: the largest m of the pairs (sizes the shared-memory staging).
-void grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
-                       int max_m, int d, cudaStream_t st);
+// Pair grids of a batch (pairs, gps: device arrays of npairs) and their
+// search orders. max_m: the largest m of the pairs (sizes the shared-memory
+// staging). Returns GridArgs::search_order for the batch.
+int grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
+                      int max_m, int d, cudaStream_t st);
 void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st);
 void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st);
 void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a, const int* cnt_b,

@@ -81,37 +81,6 @@ constexpr int kMiSlotPairs = 4096;    // concurrent MI jobs with node grids
 constexpr int kGridTickPairs = 16384; // largest tick run on cell grids
 constexpr int kGridMinSamples = 1000;
 
-size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
-
-// Bytes of one node's grid buffers (edges, cell starts, cells, order,
-// sorted coordinates) for m samples of d coordinates.
-size_t node_grid_bytes(int m, int d) {
-    const int G = grid_cells_per_axis(m);
-    return align16(2 * kGridMaxG * sizeof(float)) + grid_index_bytes(G) +
-           align16(static_cast<size_t>(m) * sizeof(unsigned short)) + align16(static_cast<size_t>(m) * sizeof(int)) +
-           align16(static_cast<size_t>(d) * m * sizeof(float));
-}
-
-// Descriptor of a node grid whose buffers start at `base`.
-GridNode node_grid_at(unsigned char* base, const float* x, int ld, int m) {
-    GridNode n{};
-    n.x = x;
-    n.ld = ld;
-    n.m = m;
-    n.G = grid_cells_per_axis(m);
-    n.e1 = reinterpret_cast<float*>(base);
-    n.e2 = n.e1 + kGridMaxG;
-    base += align16(2 * kGridMaxG * sizeof(float));
-    n.start = reinterpret_cast<int*>(base);
-    base += grid_index_bytes(n.G);
-    n.cell = reinterpret_cast<unsigned short*>(base);
-    base += align16(static_cast<size_t>(m) * sizeof(unsigned short));
-    n.perm = reinterpret_cast<int*>(base);
-    base += align16(static_cast<size_t>(m) * sizeof(int));
-    n.sx = reinterpret_cast<float*>(base);
-    return n;
-}
-
 }  // namespace
 
 double Server::now() const { return steady_seconds(); }
@@ -188,14 +157,14 @@ int Server::register_trajectory(const float* X, int N, int m, int d) {
     // node grids of every row, built once: the cell-grid search of later ticks reads them
     size_t gbytes = 0;
     if (next_node_slot_ + N <= kNodeSlots - 2 * kMiSlotPairs) {
-        const size_t per = node_grid_bytes(m, d);
+        const size_t per = grid_node_bytes(m, d);
         gbytes = per * N;
         t->grid_arena.reset(gbytes);
         t->slot0 = next_node_slot_;
         std::vector<GridNode> nodes(N);
         const size_t row = static_cast<size_t>(d) * t->ld;
         for (int a = 0; a < N; ++a) {
-            nodes[a] = node_grid_at(t->grid_arena.as<unsigned char>() + per * a, t->X.as<float>() + a * row,
+            nodes[a] = grid_node_at(t->grid_arena.as<unsigned char>() + per * a, t->X.as<float>() + a * row,
                                     t->ld, m);
         }
         GridNode* dst = d_gnodes_.as<GridNode>() + t->slot0;
@@ -349,11 +318,11 @@ bool Server::try_admit_locked(Job& j) {
         if (!free_mi_slots_.empty()) {
             j.mi_slot = free_mi_slots_.back();
             free_mi_slots_.pop_back();
-            const size_t per = node_grid_bytes(j.n, j.d);
+            const size_t per = grid_node_bytes(j.n, j.d);
             j.grid_arena.alloc(2 * per, ksg_stream_);
             GridNode nodes[2];
             for (int r = 0; r < 2; ++r) {
-                nodes[r] = node_grid_at(j.grid_arena.as<unsigned char>() + per * r,
+                nodes[r] = grid_node_at(j.grid_arena.as<unsigned char>() + per * r,
                                         j.dx.as<float>() + static_cast<size_t>(r) * j.d * j.ld, j.ld, j.n);
             }
             GridNode* dst = d_gnodes_.as<GridNode>() + j.mi_slot;
@@ -427,13 +396,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
             GridPair& g = h_gpairs_[p];
             g.a = j->slots[q].first;
             g.b = j->slots[q].second;
-            const int G = grid_cells_per_axis(pr.m);
-            g.start = reinterpret_cast<int*>(arena);
-            arena += grid_index_bytes(G);
-            g.perm = reinterpret_cast<int*>(arena);
-            arena += align16(static_cast<size_t>(pr.m) * sizeof(int));
-            g.sx = reinterpret_cast<float*>(arena);
-            arena += align16(static_cast<size_t>(2 * d) * pr.m * sizeof(float));
+            arena = grid_pair_place(g, arena, pr.m, d);
             h_wpre_[p] = static_cast<int>(wacc);
             wacc += (pr.m + 31) / 32;
             maxm = std::max(maxm, pr.m);
@@ -453,13 +416,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     ensure(d_eps_b_, sizeof(float) * samples);
     ensure(d_cnt_a_, sizeof(int) * samples);
     ensure(d_cnt_b_, sizeof(int) * samples);
-    const uintptr_t base = reinterpret_cast<uintptr_t>(d_garena_.get());
-    for (long long i = 0; i < np; ++i) {
-        GridPair& g = h_gpairs_[i];
-        g.start = reinterpret_cast<int*>(base + reinterpret_cast<uintptr_t>(g.start));
-        g.perm = reinterpret_cast<int*>(base + reinterpret_cast<uintptr_t>(g.perm));
-        g.sx = reinterpret_cast<float*>(base + reinterpret_cast<uintptr_t>(g.sx));
-    }
+    for (long long i = 0; i < np; ++i) grid_pair_rebase(h_gpairs_[i], d_garena_.get());
     NSG_CUDA(cudaMemcpyAsync(d_pairs_.get(), h_pairs_, sizeof(KsgPairDesc) * np, cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemcpyAsync(d_gpairs_.get(), h_gpairs_, sizeof(GridPair) * np, cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemcpyAsync(d_wpre_.get(), h_wpre_, sizeof(int) * (np + 1), cudaMemcpyHostToDevice, s));
@@ -477,8 +434,10 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     NSG_CUDA(cudaMemsetAsync(d_counters_.get(), 0, sizeof(int) * 4, s));
     int* ctr = d_counters_.as<int>();
     KsgPairDesc* dp = d_pairs_.as<KsgPairDesc>();
-    grid_launch_pairs(dp, d_gpairs_.as<GridPair>(), d_gnodes_.as<GridNode>(), static_cast<int>(np), maxm, d, s);
+    const int search_order =
+        grid_launch_pairs(dp, d_gpairs_.as<GridPair>(), d_gnodes_.as<GridNode>(), static_cast<int>(np), maxm, d, s);
     GridArgs a{};
+    a.search_order = search_order;
     a.pairs = dp;
     a.gp = d_gpairs_.as<GridPair>();
     a.nodes = d_gnodes_.as<GridNode>();
