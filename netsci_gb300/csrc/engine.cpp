@@ -602,6 +602,8 @@ struct KsgPlan::GridState {
     DeviceBuffer nodes, node_arena;       // GridNode[nnodes] and their buffers
     DeviceBuffer gps, pair_arena;         // GridPair per plan pair; pair grids of one batch
     std::vector<int> batch_maxm;          // largest m of each batch
+    std::vector<char> batch_order;        // whether each batch builds block orders
+    bool node_est = false;                // some batch does: nodes need scale estimates
     DeviceBuffer wprefix;                 // per batch: npairs+1 prefix of ceil(m/32)
     std::vector<long long> wprefix_off;   // offset of each batch's prefix
     DeviceBuffer groups, gprefix;         // count groups and their item prefix, per batch
@@ -674,6 +676,9 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
         }
         wpre.push_back(acc);
         g->batch_maxm.push_back(maxm);
+        const bool order = grid_orders_pay(acc, sm_count());
+        g->batch_order.push_back(order ? 1 : 0);
+        g->node_est = g->node_est || order;
         pair_arena = std::max(pair_arena, off);
     }
     g->pair_arena.reset(std::max<size_t>(pair_arena, 16));
@@ -697,7 +702,9 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
         }
         size_t corder = 0;
         for (size_t bi = 0; bi < batches_.size(); ++bi) {
-            corder = std::max(corder, static_cast<size_t>(g->ngroups[bi]) * g->batch_maxm[bi]);
+            if (g->batch_order[bi]) {
+                corder = std::max(corder, static_cast<size_t>(g->ngroups[bi]) * g->batch_maxm[bi]);
+            }
         }
         g->corder.reset(std::max<size_t>(1, corder) * sizeof(int));
         g->groups.reset(std::max<size_t>(1, groups.size()) * sizeof(CountGroup));
@@ -729,13 +736,15 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
     GridState& g = *grid_;
     NSG_CUDA(cudaMemsetAsync(g.evals.get(), 0, 2 * sizeof(unsigned long long), s));
     grid_launch_gather(gather_rows_.as<GatherRow>(), ngather_, d_, fault_.as<int>(), s);
-    grid_launch_nodes(g.nodes.as<GridNode>(), g.nnodes, d_, s);
+    grid_launch_nodes(g.nodes.as<GridNode>(), g.nnodes, d_, g.node_est, s);
     for (size_t bi = 0; bi < batches_.size(); ++bi) {
         const Batch& b = batches_[bi];
         int* ctr = counters_.as<int>() + kCounters * bi;
         KsgPairDesc* bp = pairs_dev_.as<KsgPairDesc>() + b.pair0;
         GridPair* bg = g.gps.as<GridPair>() + b.pair0;
-        const int search_order = grid_launch_pairs(bp, bg, g.nodes.as<GridNode>(), b.npairs, g.batch_maxm[bi], d_, s);
+        const bool order = g.batch_order[bi] != 0;
+        const int search_order =
+            grid_launch_pairs(bp, bg, g.nodes.as<GridNode>(), b.npairs, g.batch_maxm[bi], d_, order, s);
         GridArgs a{};
         a.search_order = search_order;
         a.pairs = bp;
@@ -761,7 +770,7 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         a.eps_x = out_.eps_x;
         a.eps_y = out_.eps_y;
         a.kdist = out_.kdist;
-        a.corder = g.corder.as<int>();
+        a.corder = order ? g.corder.as<int>() : nullptr;
         a.corder_ld = g.batch_maxm[bi];
         if (timing_) record_event(events_[2 * bi], s);
         grid_launch_search(a, d_, kmax_, g.search_grid, s);

@@ -343,14 +343,20 @@ __device__ __forceinline__ int block_zcode(int bx, int by) {
     return z;
 }
 
-// Sort key of a box size >= 0: its bits order as the values; NaN last.
-__device__ __forceinline__ unsigned order_key(float e) { return isnan(e) ? 0xffffffffu : __float_as_uint(e); }
+// Sort key of a box size e >= 0 at storage position pos < 65536: the top 16
+// bits of e (its bits order as the values; NaN last), which resolve sizes to
+// under 1%, then the position. Keys are distinct, so the ranks within a
+// block are always a permutation.
+static_assert(kOrderMaxM <= 65536, "positions fill the low 16 bits of a key");
+__device__ __forceinline__ unsigned order_key(float e, int pos) {
+    const unsigned b = isnan(e) ? 0xffffffffu : __float_as_uint(e);
+    return (b & 0xffff0000u) | static_cast<unsigned>(pos);
+}
 
 // Writes out[rank] = pos in the block order for every storage position pos
 // of a grid of G x G cells (cell index `start`), with the keys in s_key[pos]
 // and cell_of(pos, row, col) giving each position's cell. Called by the
-// whole CTA after it has written s_key. Keys with the position as tie-break
-// form a strict total order, so the ranks are always a permutation of [0, m).
+// whole CTA after it has written s_key.
 template <class CellOf>
 __device__ void write_block_order(const unsigned* s_key, const int* start, int G, int m, CellOf cell_of,
                                   int* out) {
@@ -393,10 +399,7 @@ __device__ void write_block_order(const unsigned* s_key, const int* start, int G
         int rank = 0;
         for (int r = bx * kOrderBlock; r < min((bx + 1) * kOrderBlock, G); ++r) {
             const int lo = __ldg(start + r * G + c0), hi = __ldg(start + r * G + c1);
-            for (int q = lo; q < hi; ++q) {
-                const unsigned kq = s_key[q];
-                rank += (kq < key || (kq == key && q < pos)) ? 1 : 0;
-            }
+            for (int q = lo; q < hi; ++q) rank += s_key[q] < key ? 1 : 0;
         }
         out[s_boff[block_zcode(bx, by)] + rank] = pos;
     }
@@ -418,7 +421,7 @@ __global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArg
         float e = __ldg(eps + o[0] + j);
 #pragma unroll
         for (int p = 1; p < kCountGroup; ++p) e = fmaxf(e, __ldg(eps + o[p] + j));
-        s_key[pos] = order_key(e);
+        s_key[pos] = order_key(e, pos);
     }
     const auto cell_of = [&](int pos, int& row, int& col) {
         const int c = __ldg(nd.cell + __ldg(nd.perm + pos));
@@ -440,7 +443,7 @@ __global__ void __launch_bounds__(kOrderThreads) grid_pair_order_kernel(const Ks
     const int m = pairs[blockIdx.x].m, G = na.G;
     for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
         const int j = __ldg(gp.perm + pos);
-        s_key[pos] = order_key(fmaxf(__ldg(na.est + j), __ldg(nb.est + j)));
+        s_key[pos] = order_key(fmaxf(__ldg(na.est + j), __ldg(nb.est + j)), pos);
     }
     const auto cell_of = [&](int pos, int& row, int& col) {
         const int j = __ldg(gp.perm + pos);
@@ -512,24 +515,28 @@ int grid_cells_per_axis(int m) {
     return g;
 }
 
-void grid_launch_nodes(GridNode* nodes, int nnodes, int d, cudaStream_t st) {
+void grid_launch_nodes(GridNode* nodes, int nnodes, int d, bool est, cudaStream_t st) {
     if (nnodes <= 0) return;
     switch (d) {
         case 1:
             grid_node_kernel<1><<<nnodes, kPrepThreads, 0, st>>>(nodes);
-            grid_node_est_kernel<1><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            if (est) grid_node_est_kernel<1><<<nnodes, kPrepThreads, 0, st>>>(nodes);
             break;
         case 2:
             grid_node_kernel<2><<<nnodes, kPrepThreads, 0, st>>>(nodes);
-            grid_node_est_kernel<2><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            if (est) grid_node_est_kernel<2><<<nnodes, kPrepThreads, 0, st>>>(nodes);
             break;
         case 3:
             grid_node_kernel<3><<<nnodes, kPrepThreads, 0, st>>>(nodes);
-            grid_node_est_kernel<3><<<nnodes, kPrepThreads, 0, st>>>(nodes);
+            if (est) grid_node_est_kernel<3><<<nnodes, kPrepThreads, 0, st>>>(nodes);
             break;
         default: invalid("d must be 1, 2 or 3");
     }
     NSG_CUDA(cudaGetLastError());
+}
+
+bool grid_orders_pay(long long search_warps, int sms) {
+    return search_warps >= static_cast<long long>(kOrderMinWaves) * 32 * sms;
 }
 
 size_t grid_node_bytes(int m, int d) {
@@ -608,7 +615,7 @@ void launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes
 }  // namespace
 
 int grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
-                      int max_m, int d, cudaStream_t st) {
+                      int max_m, int d, bool order, cudaStream_t st) {
     if (npairs <= 0) return 0;
     switch (d) {
         case 1: launch_pairs<1>(pairs, gps, nodes, npairs, max_m, st); break;
@@ -617,7 +624,7 @@ int grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* n
         default: invalid("d must be 1, 2 or 3");
     }
     NSG_CUDA(cudaGetLastError());
-    if (max_m > kOrderMaxM) return 0;
+    if (!order || max_m > kOrderMaxM) return 0;
     // set on every launch: the attribute belongs to the current device
     NSG_CUDA(cudaFuncSetAttribute(grid_pair_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(sizeof(unsigned) * kOrderMaxM)));

@@ -113,6 +113,12 @@ struct GridArgs {
 // keys of one grid fit in shared memory).
 constexpr int kOrderBlock = 4;
 constexpr int kOrderMaxM = 40960;
+// Orders are built for batches whose search runs at least this many waves
+// of resident warps. Below that the batch is latency-bound, and the order
+// kernels (one CTA per pair or group) sit on its critical path: one pair at
+// m = 10000 took 1.4 ms per call with them against 0.95 ms without.
+constexpr int kOrderMinWaves = 8;
+bool grid_orders_pay(long long search_warps, int sms);
 
 // A frame-mapped row copied out for the cell-grid search:
 // out[c*ld_out + s] = x[c*ld + fmap[s]] for s < m, +inf up to ld_out.
@@ -138,13 +144,15 @@ GridNode grid_node_at(unsigned char* base, const float* x, int ld, int m);
 // (pointers hold offsets until grid_pair_rebase) and returns the end offset.
 size_t grid_pair_place(GridPair& g, size_t off, int m, int d);
 void grid_pair_rebase(GridPair& g, const void* base);
-// Node grids (nodes: device array whose x, ld, m, G and buffers are set).
-void grid_launch_nodes(GridNode* nodes, int nnodes, int d, cudaStream_t st);
-// Pair grids of a batch (pairs, gps: device arrays of npairs) and their
-// search orders. max_m: the largest m of the pairs (sizes the shared-memory
-// staging). Returns GridArgs::search_order for the batch.
+// Node grids (nodes: device array whose x, ld, m, G and buffers are set),
+// with their scale estimates when `est` (needed by the search orders).
+void grid_launch_nodes(GridNode* nodes, int nnodes, int d, bool est, cudaStream_t st);
+// Pair grids of a batch (pairs, gps: device arrays of npairs) and, when
+// `order` (the nodes carry scale estimates), their search orders. max_m: the
+// largest m of the pairs (sizes the shared-memory staging). Returns
+// GridArgs::search_order for the batch.
 int grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
-                      int max_m, int d, cudaStream_t st);
+                      int max_m, int d, bool order, cudaStream_t st);
 void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st);
 void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st);
 void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a, const int* cnt_b,

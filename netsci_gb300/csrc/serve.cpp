@@ -169,7 +169,7 @@ int Server::register_trajectory(const float* X, int N, int m, int d) {
         }
         GridNode* dst = d_gnodes_.as<GridNode>() + t->slot0;
         NSG_CUDA(cudaMemcpy(dst, nodes.data(), sizeof(GridNode) * N, cudaMemcpyHostToDevice));
-        grid_launch_nodes(dst, N, d, nullptr);
+        grid_launch_nodes(dst, N, d, true, nullptr);
         NSG_CUDA(cudaDeviceSynchronize());
         next_node_slot_ += N;
     } else {
@@ -328,7 +328,7 @@ bool Server::try_admit_locked(Job& j) {
             GridNode* dst = d_gnodes_.as<GridNode>() + j.mi_slot;
             NSG_CUDA(cudaMemcpyAsync(dst, nodes, sizeof(nodes), cudaMemcpyHostToDevice, ksg_stream_));
             NSG_CUDA(cudaStreamSynchronize(ksg_stream_));  // the host descriptors go out of scope
-            grid_launch_nodes(dst, 2, j.d, ksg_stream_);
+            grid_launch_nodes(dst, 2, j.d, true, ksg_stream_);
             j.slots.push_back({j.mi_slot, j.mi_slot + 1});
         }
     }
@@ -427,15 +427,18 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         gpre[gi + 1] = gpre[gi] + (h_pairs_[groups[gi].pairs[0]].m + kCountQueries - 1) / kCountQueries;
     }
-    ensure(d_corder_, sizeof(int) * std::max<size_t>(1, groups.size() * static_cast<size_t>(maxm)));
+    if (grid_orders_pay(wacc, sm_count())) {
+        ensure(d_corder_, sizeof(int) * std::max<size_t>(1, groups.size() * static_cast<size_t>(maxm)));
+    }
     NSG_CUDA(cudaMemcpyAsync(d_groups_.get(), groups.data(), sizeof(CountGroup) * groups.size(),
                              cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemcpyAsync(d_gpre_.get(), gpre.data(), sizeof(int) * gpre.size(), cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemsetAsync(d_counters_.get(), 0, sizeof(int) * 4, s));
     int* ctr = d_counters_.as<int>();
     KsgPairDesc* dp = d_pairs_.as<KsgPairDesc>();
-    const int search_order =
-        grid_launch_pairs(dp, d_gpairs_.as<GridPair>(), d_gnodes_.as<GridNode>(), static_cast<int>(np), maxm, d, s);
+    const bool order = grid_orders_pay(wacc, sm_count());
+    const int search_order = grid_launch_pairs(dp, d_gpairs_.as<GridPair>(), d_gnodes_.as<GridNode>(),
+                                               static_cast<int>(np), maxm, d, order, s);
     GridArgs a{};
     a.search_order = search_order;
     a.pairs = dp;
@@ -457,7 +460,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     a.eps_b = d_eps_b_.as<float>();
     a.cnt_a = d_cnt_a_.as<int>();
     a.cnt_b = d_cnt_b_.as<int>();
-    a.corder = d_corder_.as<int>();
+    a.corder = order ? d_corder_.as<int>() : nullptr;
     a.corder_ld = maxm;
     const int sms = sm_count();
     grid_launch_search(a, d, kmax, sms * grid_search_ctas_per_sm(d, kmax), s);
