@@ -22,11 +22,13 @@
 //     with the two nodes' edges, both nodes' coordinates copied in that
 //     order with the frames' original indices.
 //
-// Warps, not CTAs, own queries: a warp takes 32 frames consecutive in the
-// grid's query order (Z order of the cells) as its queries, so their boxes
-// overlap, and
-// streams the frames of the cells it must visit through its own slice of
-// shared memory, 128 frames at a time, read back as float4 broadcasts.
+// Warps, not CTAs, own queries: a warp takes frames consecutive in a query
+// order as its queries (32 in pass 1, 16 at two lanes each in the counts).
+// The order is a block order where the batch builds one (4 x 4 cell blocks
+// in Z order, queries within a block by box size, ksg_grid.cu), else the Z
+// order of the cells. The queries' boxes then overlap. The warp streams the
+// frames of the cells it must visit through its own slice of shared memory,
+// read back as float4 (pass 1) or float2 (counts) broadcasts.
 // Pass 1 first scans the rectangle of cells its queries sit in (the seed,
 // which fills the neighbour lists and bounds U), then cell rows outward,
 // recomputing each row's column range from the current bounds and stopping
