@@ -427,16 +427,14 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         gpre[gi + 1] = gpre[gi] + (h_pairs_[groups[gi].pairs[0]].m + kCountQueries - 1) / kCountQueries;
     }
-    if (grid_orders_pay(wacc, sm_count())) {
-        ensure(d_corder_, sizeof(int) * std::max<size_t>(1, groups.size() * static_cast<size_t>(maxm)));
-    }
+    const bool order = grid_orders_pay(wacc, sm_count());  // block orders for this tick
+    if (order) ensure(d_corder_, sizeof(int) * std::max<size_t>(1, groups.size() * static_cast<size_t>(maxm)));
     NSG_CUDA(cudaMemcpyAsync(d_groups_.get(), groups.data(), sizeof(CountGroup) * groups.size(),
                              cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemcpyAsync(d_gpre_.get(), gpre.data(), sizeof(int) * gpre.size(), cudaMemcpyHostToDevice, s));
     NSG_CUDA(cudaMemsetAsync(d_counters_.get(), 0, sizeof(int) * 4, s));
     int* ctr = d_counters_.as<int>();
     KsgPairDesc* dp = d_pairs_.as<KsgPairDesc>();
-    const bool order = grid_orders_pay(wacc, sm_count());
     const int search_order = grid_launch_pairs(dp, d_gpairs_.as<GridPair>(), d_gnodes_.as<GridNode>(),
                                                static_cast<int>(np), maxm, d, order, s);
     GridArgs a{};
