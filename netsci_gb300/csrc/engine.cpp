@@ -811,6 +811,22 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
     }
 }
 
+int KsgPlan::launches() const {
+    const int nb = static_cast<int>(batches_.size());
+    if (search_ != 1) return 3 * nb;
+    if (!nb) return 0;
+    // node grids (+ scale estimates), gather; per batch: pair grids, search,
+    // counts, combine, ties, final sums (+ search and count orders)
+    int n = 1 + (ngather_ ? 1 : 0) + 6 * nb;
+    if (grid_) {
+        if (grid_->node_est) ++n;
+        for (size_t bi = 0; bi < grid_->batch_order.size(); ++bi) {
+            if (grid_->batch_order[bi] && grid_->batch_maxm[bi] <= kOrderMaxM) n += 2;
+        }
+    }
+    return n;
+}
+
 int KsgPlan::staging() const { return entry_ ? entry_->tma : 0; }
 
 void KsgPlan::evaluations(unsigned long long* search, unsigned long long* counts) const {

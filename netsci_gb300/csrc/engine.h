@@ -78,10 +78,7 @@ public:
     // Kernel launches per run: count, tie resolution and finalize per batch
     // (exhaustive search); node grids once, then pair grids, search, counts,
     // combine, ties and finalize per batch (cell-grid search).
-    int launches() const {
-        const int nb = static_cast<int>(batches_.size());
-        return search_ == 1 ? (nb ? 1 + (ngather_ ? 1 : 0) + 6 * nb : 0) : 3 * nb;
-    }
+    int launches() const;
     // Device time of the count kernels of the last run (ms); needs timing.
     float count_ms() const;
     long long pairs() const { return npairs_; }
