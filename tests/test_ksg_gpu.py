@@ -155,8 +155,15 @@ def test_protein56_device_plan_graph(golden, oracle_mod):
         torch.cuda.synchronize()
         assert np.array_equal(gc.cpu().numpy(), g1)
     # exhaustive: count, ties, finalize; cell grids (m = 1000 selects them):
-    # node grids, pair grids, search, counts, combine, ties, finalize
-    assert plan.launches == (7 if plan.shape["search"] == "cell-grid" else 3)
+    # node grids, pair grids, search, counts, combine, ties, finalize, and
+    # for a batch of at least eight waves of search warps (32 per SM) the node
+    # scale estimates and the search and count orders
+    if plan.shape["search"] == "cell-grid":
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        ordered = len(pairs) * ((1000 + 31) // 32) >= 8 * 32 * sms
+        assert plan.launches == 7 + (3 if ordered else 0)
+    else:
+        assert plan.launches == 3
 
 
 def test_uneven_trajectories_one_plan(oracle_mod):
