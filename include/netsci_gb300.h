@@ -232,6 +232,13 @@ int nsg_ksg_set_staging(int staging);
  * automatic (cell grids when no pair has a frame map and at least half of
  * the work, counted as m^2 per pair, is in pairs with m >= 1000). */
 int nsg_ksg_set_search(int mode);
+/* Query orders of later cell-grid plans: 1 = always build the block orders
+ * (the search and count orders of a batch), 0 = never (cells in Z order),
+ * -1 = automatic (only for batches whose search runs at least eight waves
+ * of resident warps, where the order kernels pay for themselves). Orders
+ * change which frames are visited first, never a result; m above 40960
+ * always takes the Z order. Tuning knob with no reference counterpart.    */
+int nsg_ksg_set_orders(int mode);
 /* *mode = 1 when the plan uses cell grids, 0 when exhaustive. */
 int nsg_ksg_plan_search(const nsg_ksg_plan* plan, int* mode);
 /* Query-frame distance evaluations of the plan's last run with cell grids:

@@ -133,6 +133,7 @@ _SIGNATURES = {
     "nsg_ksg_set_staging": (c_int, [c_int]),
     "nsg_ksg_plan_staging": (c_int, [c_void_p, P_int]),
     "nsg_ksg_set_search": (c_int, [c_int]),
+    "nsg_ksg_set_orders": (c_int, [c_int]),
     "nsg_ksg_plan_search": (c_int, [c_void_p, P_int]),
     "nsg_ksg_plan_evaluations": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_ulonglong),
                                          ctypes.POINTER(ctypes.c_ulonglong)]),

@@ -567,6 +567,13 @@ int nsg_ksg_set_search(int mode) {
     });
 }
 
+int nsg_ksg_set_orders(int mode) {
+    return guarded([&] {
+        if (mode < -1 || mode > 1) nsg::invalid("orders must be -1, 0 or 1");
+        nsg::ksg_force_orders(mode);
+    });
+}
+
 int nsg_apsp_lengths_device(const float* A, float* H, int n, int L, int* steps, void* stream) {
     return guarded([&] {
         const int s = nsg::apsp_lengths(A, H, n, L, stream_of(stream));

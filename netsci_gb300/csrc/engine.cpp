@@ -161,6 +161,7 @@ KsgShape g_forced{0, 0, 0};
 int g_forced_variant = -1;
 int g_forced_staging = -1;
 int g_forced_search = -1;
+int g_forced_orders = -1;
 // Below this many samples per pair the exhaustive kernel is used: grids of
 // a few cells per axis prune little (measured: 0.91x at m = 300, 1.08x at
 // m = 1000, 1.28x at m = 2000, whole plans of 48-node trajectories).
@@ -203,6 +204,16 @@ void ksg_force_shape(int threads, int r, int frames, int variant) {
 void ksg_force_search(int mode) {
     std::lock_guard<std::mutex> lk(g_shape_mu);
     g_forced_search = mode;
+}
+
+void ksg_force_orders(int mode) {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    g_forced_orders = mode;
+}
+
+int ksg_forced_orders() {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    return g_forced_orders;
 }
 
 void ksg_force_staging(int staging) {
@@ -676,7 +687,8 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
         }
         wpre.push_back(acc);
         g->batch_maxm.push_back(maxm);
-        const bool order = grid_orders_pay(acc, sm_count());
+        const int forced = ksg_forced_orders();
+        const bool order = forced >= 0 ? forced == 1 : grid_orders_pay(acc, sm_count());
         g->batch_order.push_back(order ? 1 : 0);
         g->node_est = g->node_est || order;
         pair_arena = std::max(pair_arena, off);

@@ -151,6 +151,10 @@ void ksg_force_staging(int staging);
 // Search override set by nsg_ksg_set_search (-1 automatic, 0 exhaustive,
 // 1 cell grids).
 void ksg_force_search(int mode);
+// Block-order override for cell-grid plans set by nsg_ksg_set_orders (-1
+// automatic, 0 never, 1 always).
+void ksg_force_orders(int mode);
+int ksg_forced_orders();
 // True when every pair allows bulk-copy staging (16-byte aligned rows,
 // plane stride a multiple of 4, no frame map).
 bool ksg_bulk_copy_ok(const std::vector<nsg_ksg_pair>& pairs);

@@ -115,9 +115,11 @@ void npy_write(const std::string& path, const void* data, const std::string& des
         count *= shape[i];
     }
     dict += "), }";
-    // pad so that magic(6) + version(2) + len(2) + dict + '\n' is a multiple of 64
+    // pad so that magic(6) + version(2) + len(2) + dict + '\n' is a multiple
+    // of 16: the header length the reference's files carry (cnpy), so that
+    // checkpoint files are byte-identical to the reference's
     size_t total = 10 + dict.size() + 1;
-    dict.append((64 - total % 64) % 64, ' ');
+    dict.append((16 - total % 16) % 16, ' ');
     dict += '\n';
     FilePtr f(std::fopen(path.c_str(), "wb"));
     if (!f) io_fail("cannot write " + path);

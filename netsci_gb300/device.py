@@ -178,6 +178,11 @@ def set_ksg_search(mode: int = -1) -> None:
     call("nsg_ksg_set_search", int(mode))
 
 
+def set_ksg_orders(mode: int = -1) -> None:
+    """Block query orders of later cell-grid plans: 1 always, 0 never, -1 automatic."""
+    call("nsg_ksg_set_orders", int(mode))
+
+
 def apsp_lengths(A: torch.Tensor, max_path_length: int, H: torch.Tensor | None = None,
                  stream: torch.cuda.Stream | None = None) -> tuple[torch.Tensor, int]:
     n = A.shape[0]

@@ -24,16 +24,48 @@ _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 
+REPO = HERE.parent
+
+
+def ref_root() -> Path:
+    """Where the reference sources are compiled from: NETSCI_REF, else the
+    copy that ``make -C oracle stage`` leaves in baseline/_ref/netsci."""
+    return Path(os.environ.get("NETSCI_REF", str(REPO / "baseline" / "_ref" / "netsci")))
+
+
+def have_ref_sources() -> bool:
+    return Path(ref_root(), "netcalc", "src").is_dir()
+
+
 def build(ref: bool | None = None) -> None:
-    """Compile the restatement (and the reference CPU library when its
+    """Compile the restatement (and the reference CPU libraries when their
     sources are present, or when ``ref`` is True)."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
-    ref_root = os.environ.get("NETSCI_REF", "/root/reference")
     if ref is None:
-        ref = Path(ref_root, "netcalc", "src").is_dir()
+        ref = have_ref_sources()
     if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"NETSCI_REF={ref_root}"],
+        subprocess.run(["make", "-s", "-j4", "-C", str(HERE), "ref", f"NETSCI_REF={ref_root()}"],
                        check=True)
+
+
+def start_ref_gpu_build():
+    """Start compiling the reference's GPU code for sm_103a in the background
+    (about half a minute); returns the process, or None when the sources are
+    absent. ``finish_ref_gpu_build`` waits for it."""
+    if not have_ref_sources():
+        return None
+    jobs = str(max(2, min(8, os.cpu_count() or 2)))
+    return subprocess.Popen(["make", "-s", f"-j{jobs}", "-C", str(HERE), "ref-gpu",
+                             f"NETSCI_REF={ref_root()}"],
+                            stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+
+
+def finish_ref_gpu_build(proc) -> None:
+    if proc is None:
+        return
+    out, _ = proc.communicate()
+    if proc.returncode != 0:
+        raise RuntimeError(f"make ref-gpu failed:\n{out}")
 
 
 def lib():
@@ -50,6 +82,8 @@ def lib():
             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
             ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_mi_pair.restype = ctypes.c_float
+        L.oracle_mi_pair_mt.argtypes = L.oracle_mi_pair.argtypes + [ctypes.c_int]
+        L.oracle_mi_pair_mt.restype = ctypes.c_float
         L.oracle_mi_from_counts.argtypes = [_i32p, _i32p, ctypes.c_int, ctypes.c_int, _f32p]
         L.oracle_mi_from_counts.restype = ctypes.c_float
         L.oracle_gc_from_mi.argtypes = [ctypes.c_float, ctypes.c_int]
@@ -90,8 +124,66 @@ def ref_lib():
             fn.restype = ctypes.c_float
         R.ref_psi.argtypes = [_f32p, ctypes.c_int]
         R.ref_psi.restype = None
+        R.ref_pairs_checkpoint.argtypes = [_f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_char_p, _f32p]
+        R.ref_pairs_checkpoint.restype = ctypes.c_int
+        R.ref_restart_ab.argtypes = [_i32p, ctypes.c_int, ctypes.c_char_p, _i32p, ctypes.c_int]
+        R.ref_restart_ab.restype = ctypes.c_int
         _REF = R
     return _REF
+
+
+_REF_GPU = None
+
+
+def ref_gpu_lib():
+    """The reference's GPU functions (``_ref/libnetcalc_ref_gpu.so``), or None
+    when that library was not built."""
+    global _REF_GPU
+    if _REF_GPU is None:
+        path = HERE / "_ref" / "libnetcalc_ref_gpu.so"
+        if not path.exists():
+            return None
+        G = ctypes.CDLL(str(path))
+        for name in ("refgpu_mi", "refgpu_gc"):
+            fn = getattr(G, name)
+            fn.argtypes = [_f32p, _f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+            fn.restype = ctypes.c_float
+        G.refgpu_apsp_lengths.argtypes = [_f32p, _f32p, ctypes.c_int, ctypes.c_int]
+        G.refgpu_apsp_lengths.restype = None
+        _REF_GPU = G
+    return _REF_GPU
+
+
+def ref_gpu_apsp_lengths(A, max_path_length: int) -> np.ndarray:
+    """The reference kernel's shortest-path lengths after max_path_length
+    launches (hedetniemi_gpu.cu:109-146)."""
+    A = _c(A, np.float32)
+    H = np.zeros_like(A)
+    ref_gpu_lib().refgpu_apsp_lengths(A.ravel(), H.ravel(), A.shape[0], int(max_path_length))
+    return H
+
+
+def ref_pairs_checkpoint(X, n: int, d: int, ab, k: int, gc: bool, frequency: int,
+                         file_name: str):
+    """The reference pair-list driver with checkpoint files, CPU platform
+    (mutual_information.cpp:8-101 / generalized_correlation.cpp:8-102)."""
+    X = _c(X, np.float32)
+    ab = _c(ab, np.int32).reshape(-1, 2)
+    out = np.zeros(ab.shape[0], np.float32)
+    rc = ref_lib().ref_pairs_checkpoint(X.ravel(), X.shape[0], n, d, ab.ravel(), ab.shape[0], k,
+                                        int(gc), int(frequency), file_name.encode(), out)
+    return rc, out
+
+
+def ref_restart_ab(ab, checkpoint_file_name: str) -> np.ndarray:
+    """generateRestartAbFromCheckpointFile (mutual_information.cpp:174-201)."""
+    ab = _c(ab, np.int32).reshape(-1, 2)
+    out = np.zeros_like(ab)
+    m = ref_lib().ref_restart_ab(ab.ravel(), ab.shape[0], checkpoint_file_name.encode(),
+                                 out.reshape(-1), ab.shape[0])
+    return out[:m]
 
 
 def _c(a, dtype):
@@ -104,24 +196,26 @@ def psi(n: int) -> np.ndarray:
     return out
 
 
-def mi_pair(xa, xb, n: int, k: int, d: int, detail: bool = False):
-    """KSG MI of one pair. With ``detail`` also returns a dict of per-sample
-    n_x, n_y, eps_x, eps_y, kdist and the tie count."""
+def mi_pair(xa, xb, n: int, k: int, d: int, detail: bool = False, threads: int = 1):
+    """KSG MI of one pair, its samples spread over ``threads`` host threads
+    (the result does not depend on the thread count). With ``detail`` also
+    returns a dict of per-sample n_x, n_y, eps_x, eps_y, kdist and the tie
+    count."""
     xa = _c(xa, np.float32).ravel()
     xb = _c(xb, np.float32).ravel()
     table = psi(n)
     if not detail:
-        return float(lib().oracle_mi_pair(xa, xb, n, k, d, table, None, None, None, None,
-                                          None, None))
+        return float(lib().oracle_mi_pair_mt(xa, xb, n, k, d, table, None, None, None, None,
+                                             None, None, int(threads)))
     nx = np.zeros(n, np.int32)
     ny = np.zeros(n, np.int32)
     ex = np.zeros(n, np.float32)
     ey = np.zeros(n, np.float32)
     kd = np.zeros(n, np.float32)
     ties = ctypes.c_int(0)
-    mi = lib().oracle_mi_pair(xa, xb, n, k, d, table, nx.ctypes.data, ny.ctypes.data,
-                              ex.ctypes.data, ey.ctypes.data, kd.ctypes.data,
-                              ctypes.addressof(ties))
+    mi = lib().oracle_mi_pair_mt(xa, xb, n, k, d, table, nx.ctypes.data, ny.ctypes.data,
+                                 ex.ctypes.data, ey.ctypes.data, kd.ctypes.data,
+                                 ctypes.addressof(ties), int(threads))
     return float(mi), dict(n_x=nx, n_y=ny, eps_x=ex, eps_y=ey, kdist=kd, ties=ties.value)
 
 

@@ -65,8 +65,59 @@ void oracle_psi(float* psi, int n) {
     }
 }
 
-// KSG (algorithm 2) mutual information of one variable pair.
-// netcalc/src/mutual_information_cpu.cpp:6-121.
+// One sample's KSG terms: the joint-distance row, the reference's sort, eps
+// over sorted positions 1..k and the marginal counts.
+// netcalc/src/mutual_information_cpu.cpp:27-109 (one iteration of its loop
+// over samples). Returns 1 when the sample's neighbour set is decided by the
+// tie rule (equal k-th and (k+1)-th joint distances with different
+// marginals), else 0.
+static int sample_terms(const float* xa, const float* xb, int n, int k, int d, int i,
+                        Scratch& s, int* cx_out, int* cy_out, float* ex_out, float* ey_out,
+                        float* kd_out) {
+    // joint distances, :27-47
+    for (int j = 0; j < n; ++j) {
+        float da = marginal(xa, n, d, i, j);
+        float db = marginal(xb, n, d, i, j);
+        s.dz[j] = std::max(da, db);
+    }
+    // ascending order, :48-53 (the reference's comparator)
+    std::iota(s.order.begin(), s.order.end(), 0);
+    const float* dz = s.dz.data();
+    std::sort(s.order.begin(), s.order.end(), [dz](int a, int b) { return dz[a] < dz[b]; });
+    // eps over sorted positions 1..k, :54-77
+    float ex = 0.0f, ey = 0.0f;
+    for (int q = 1; q < k + 1; ++q) {
+        int j = s.order[q];
+        ex = std::max(ex, marginal(xa, n, d, i, j));
+        ey = std::max(ey, marginal(xb, n, d, i, j));
+    }
+    int tie = 0;
+    if (k + 1 < n) {
+        int jk = s.order[k], jn = s.order[k + 1];
+        if (dz[jk] == dz[jn] &&
+            (marginal(xa, n, d, i, jk) != marginal(xa, n, d, i, jn) ||
+             marginal(xb, n, d, i, jk) != marginal(xb, n, d, i, jn))) {
+            tie = 1;
+        }
+    }
+    // marginal counts over all j (self included), then -1, :78-109
+    int cx = 0, cy = 0;
+    for (int j = 0; j < n; ++j) {
+        if (marginal(xa, n, d, i, j) <= ex) ++cx;
+        if (marginal(xb, n, d, i, j) <= ey) ++cy;
+    }
+    *cx_out = cx - 1;
+    *cy_out = cy - 1;
+    *ex_out = ex;
+    *ey_out = ey;
+    *kd_out = dz[s.order[k]];
+    return tie;
+}
+
+// KSG (algorithm 2) mutual information of one variable pair, with the
+// samples spread over `threads` host threads; the per-sample terms are
+// summed afterwards in sample order, so the result does not depend on the
+// thread count. netcalc/src/mutual_information_cpu.cpp:6-121.
 //   xa, xb : d planes of n samples each (plane-major rows of X)
 //   psi    : table from oracle_psi(psi, n)
 // Optional per-sample outputs (may be null): n_x, n_y (marginal counts after
@@ -74,61 +125,53 @@ void oracle_psi(float* psi, int n) {
 // nearest joint neighbours), kdist (k-th smallest joint distance, self
 // excluded). ties (may be null) receives the number of samples whose
 // neighbour set is decided by the tie rule.
-float oracle_mi_pair(const float* xa, const float* xb, int n, int k, int d,
-                     const float* psi, int* n_x, int* n_y, float* eps_x,
-                     float* eps_y, float* kdist, int* ties) {
-    Scratch s;
-    s.dz.resize(n);
-    s.order.resize(n);
-    int tie_count = 0;
-    float average = 0.0f;
-    for (int i = 0; i < n; ++i) {
-        // joint distances, :27-47
-        for (int j = 0; j < n; ++j) {
-            float da = marginal(xa, n, d, i, j);
-            float db = marginal(xb, n, d, i, j);
-            s.dz[j] = std::max(da, db);
+float oracle_mi_pair_mt(const float* xa, const float* xb, int n, int k, int d,
+                        const float* psi, int* n_x, int* n_y, float* eps_x,
+                        float* eps_y, float* kdist, int* ties, int threads) {
+    std::vector<int> cx(n), cy(n);
+    std::vector<float> ex(n), ey(n), kd(n);
+    std::atomic<int> tie_count(0);
+    if (threads < 1) threads = 1;
+    if (threads > n) threads = n > 0 ? n : 1;
+    auto work = [&](int t) {
+        Scratch s;
+        s.dz.resize(n);
+        s.order.resize(n);
+        int local = 0;
+        for (int i = t; i < n; i += threads) {
+            local += sample_terms(xa, xb, n, k, d, i, s, &cx[i], &cy[i], &ex[i], &ey[i], &kd[i]);
         }
-        // ascending order, :48-53 (the reference's comparator)
-        std::iota(s.order.begin(), s.order.end(), 0);
-        const float* dz = s.dz.data();
-        std::sort(s.order.begin(), s.order.end(), [dz](int a, int b) { return dz[a] < dz[b]; });
-        // eps over sorted positions 1..k, :54-77
-        float ex = 0.0f, ey = 0.0f;
-        for (int q = 1; q < k + 1; ++q) {
-            int j = s.order[q];
-            ex = std::max(ex, marginal(xa, n, d, i, j));
-            ey = std::max(ey, marginal(xb, n, d, i, j));
-        }
-        if (k + 1 < n) {
-            int jk = s.order[k], jn = s.order[k + 1];
-            if (dz[jk] == dz[jn] &&
-                (marginal(xa, n, d, i, jk) != marginal(xa, n, d, i, jn) ||
-                 marginal(xb, n, d, i, jk) != marginal(xb, n, d, i, jn))) {
-                ++tie_count;
-            }
-        }
-        // marginal counts over all j (self included), then -1, :78-109
-        int cx = 0, cy = 0;
-        for (int j = 0; j < n; ++j) {
-            if (marginal(xa, n, d, i, j) <= ex) ++cx;
-            if (marginal(xb, n, d, i, j) <= ey) ++cy;
-        }
-        cx -= 1;
-        cy -= 1;
-        if (n_x) n_x[i] = cx;
-        if (n_y) n_y[i] = cy;
-        if (eps_x) eps_x[i] = ex;
-        if (eps_y) eps_y[i] = ey;
-        if (kdist) kdist[i] = dz[s.order[k]];
-        // float accumulation in sample order, :110
-        average += (psi[cx] + psi[cy]);
+        tie_count += local;
+    };
+    if (threads == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < threads; ++t) pool.emplace_back(work, t);
+        for (auto& th : pool) th.join();
     }
-    if (ties) *ties = tie_count;
+    // float accumulation in sample order, :110
+    float average = 0.0f;
+    for (int i = 0; i < n; ++i) average += (psi[cx[i]] + psi[cy[i]]);
+    for (int i = 0; i < n; ++i) {
+        if (n_x) n_x[i] = cx[i];
+        if (n_y) n_y[i] = cy[i];
+        if (eps_x) eps_x[i] = ex[i];
+        if (eps_y) eps_y[i] = ey[i];
+        if (kdist) kdist[i] = kd[i];
+    }
+    if (ties) *ties = tie_count.load();
     // :113-118
     average /= static_cast<float>(n);
     float mi = psi[n] + psi[k] - static_cast<float>(1.0 / static_cast<float>(k)) - average;
     return mi;
+}
+
+// The same on the calling thread only.
+float oracle_mi_pair(const float* xa, const float* xb, int n, int k, int d,
+                     const float* psi, int* n_x, int* n_y, float* eps_x,
+                     float* eps_y, float* kdist, int* ties) {
+    return oracle_mi_pair_mt(xa, xb, n, k, d, psi, n_x, n_y, eps_x, eps_y, kdist, ties, 1);
 }
 
 // MI from per-sample counts, in the reference's float summation order.

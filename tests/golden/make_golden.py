@@ -1,7 +1,8 @@
 """Generate the committed golden fixtures in tests/golden/.
 
-Run in a checkout that has the reference sources (default /root/reference,
-override with NETSCI_REF); it builds oracle/_ref from them and records the
+Run in a checkout that has the reference sources (the copy that
+``make -C oracle stage`` leaves in baseline/_ref/netsci, or NETSCI_REF); it
+builds oracle/_ref from them and records the
 reference CPU functions' outputs on fixed inputs:
 
 * gaussian.npz -- the reference's own bivariate-Gaussian test data
@@ -38,7 +39,7 @@ sys.path.insert(0, str(ROOT))
 import oracle  # noqa: E402
 from netsci_gb300 import synthetic  # noqa: E402
 
-REF = Path(os.environ.get("NETSCI_REF", "/root/reference"))
+REF = oracle.ref_root()
 GOLDEN_MI = {1000: 0.8449974060058594, 2000: 0.8485465049743652}
 
 

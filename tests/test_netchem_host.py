@@ -10,7 +10,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-REF = Path(os.environ.get("NETSCI_REF", "/root/reference"))
+REF = Path(os.environ.get("NETSCI_REF", str(Path(__file__).resolve().parent.parent / "baseline" / "_ref" / "netsci")))
 REF_FILES = [
     (REF / "tests/netchem/cpp/data/test.dcd", REF / "tests/netchem/cpp/data/test.pdb"),
     (REF / "tutorial/protG_short.dcd", REF / "tutorial/protG_short.pdb"),
