@@ -239,14 +239,29 @@ int nsg_ksg_set_search(int mode);
  * change which frames are visited first, never a result; m above 40960
  * always takes the Z order. Tuning knob with no reference counterpart.    */
 int nsg_ksg_set_orders(int mode);
+/* Issue ceilings of the cell-grid kernels, measured on the current device:
+ * the operation rate (Gop/s) of the search kernel's and the count kernel's
+ * inner loops alone (their own distance arithmetic on a staged tile, with no
+ * memory traffic, no range setup and no neighbour-list updates), counted as
+ * the kernels' rates are (search: 4d per joint distance; counts: 2d-1 per
+ * one-variable distance plus one per eps comparison). A diagnostic for the
+ * roofline of those kernels; no reference counterpart. Takes about 0.1 s. */
+int nsg_measure_issue_ceiling(int d, double* search_gops, double* count_gops);
 /* *mode = 1 when the plan uses cell grids, 0 when exhaustive. */
 int nsg_ksg_plan_search(const nsg_ksg_plan* plan, int* mode);
-/* Query-frame distance evaluations of the plan's last run with cell grids:
- * joint distances of the search, one-variable distances of the counts (an
- * exhaustive run evaluates m*m of each kind per pair). 0 for exhaustive
- * plans. Synchronizes with the device. */
+/* Query-frame evaluations of the plan's last run with cell grids: *search
+ * joint distances of the search, *counts one-variable distances of the
+ * counts (one per query and frame, shared by the pairs of a count group),
+ * *compares (may be null) the counts' eps comparisons (one per query, frame
+ * and pair of the group). An exhaustive run evaluates m*m of each kind per
+ * pair; 0 for exhaustive plans. Synchronizes with the device. */
 int nsg_ksg_plan_evaluations(const nsg_ksg_plan* plan, unsigned long long* search,
-                             unsigned long long* counts);
+                             unsigned long long* counts, unsigned long long* compares);
+/* Device milliseconds of the last run's search kernels and count kernels
+ * (flag bit 1), summed over the plan's batches; the order kernels are not
+ * included. An exhaustive plan's single kernel counts as search. Waits for
+ * that run's events. */
+int nsg_ksg_plan_kernel_ms(const nsg_ksg_plan* plan, float* search_ms, float* count_ms);
 
 /* One pair's MI / GC without any device allocation. No counterpart in the
  * reference: it is for callers that cannot allocate device memory, such as
@@ -268,11 +283,22 @@ int nsg_ksg_pair_noalloc_device(const float* xa, const float* xb, int ld, int m,
 
 /* Hedetniemi shortest path lengths on the device (A, H: n x n device
  * floats). H_{t+1}[i][j] = min_k A[j][k] + H_t[k][i] from H_0 = A, until H
- * stops changing or max_path_length steps; the steps run go to *steps
- * (host, nullable). netcalc/src/hedetniemi_gpu.cu:109-146. Synchronizes
- * `stream` once at the end to read the step count.                       */
+ * stops changing or max_path_length steps. netcalc/src/hedetniemi_gpu.cu:
+ * 109-146. Where max_path_length >= n-1 and A is symmetric with a zero
+ * diagonal, no negative weight and integer weights whose path sums stay
+ * below 2^24, the same fixed point is reached by repeated squaring
+ * (H <- H (x) H, about log2 of the hop diameter products), bit for bit.
+ * *steps (host, nullable) receives the min-plus products run (steps or
+ * squarings). Synchronizes `stream` to read flags.                       */
 int nsg_apsp_lengths_device(const float* A, float* H, int n, int max_path_length, int* steps,
                             void* stream);
+/* Product schedule of later shortest-path solves: -1 automatic (squaring
+ * only where it is bit-exact, as above), 0 Jacobi steps always (the
+ * reference's association of every path sum), 1 squaring wherever the
+ * fixed point of a symmetric, zero-diagonal, non-negative A is asked for
+ * (float weights then agree with the reference within the rounding of a
+ * path sum). Tuning knob with no reference counterpart.                  */
+int nsg_apsp_set_method(int method);
 /* Shortest paths with snapshots: paths device int[n*max_path_length*n],
  * layout paths[i*L*n + j*L + p]. netcalc/src/hedetniemi_gpu.cu:148-235. */
 int nsg_apsp_paths_device(const float* A, float* H, int* paths, int n, int max_path_length,

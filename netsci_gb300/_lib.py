@@ -134,8 +134,14 @@ _SIGNATURES = {
     "nsg_ksg_plan_staging": (c_int, [c_void_p, P_int]),
     "nsg_ksg_set_search": (c_int, [c_int]),
     "nsg_ksg_set_orders": (c_int, [c_int]),
+    "nsg_apsp_set_method": (c_int, [c_int]),
+    "nsg_measure_issue_ceiling": (c_int, [c_int, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)]),
     "nsg_ksg_plan_search": (c_int, [c_void_p, P_int]),
+    "nsg_ksg_plan_kernel_ms": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float),
+                                       ctypes.POINTER(ctypes.c_float)]),
     "nsg_ksg_plan_evaluations": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_ulonglong),
+                                         ctypes.POINTER(ctypes.c_ulonglong),
                                          ctypes.POINTER(ctypes.c_ulonglong)]),
     "nsg_server_create": (c_int, [c_size_t, c_double, c_int, PP_void]),
     "nsg_server_destroy": (c_int, [c_void_p]),

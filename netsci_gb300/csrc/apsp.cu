@@ -28,9 +28,25 @@
 // Convergence: step t writes changed[t] = 1 when any entry differs from the
 // previous iterate; step t+1 returns at once when changed[t] == 0 (the
 // iterate is then a fixed point and both buffers hold it).
+//
+// Repeated squaring. When the path length is unbounded (maxPathLength >=
+// n-1) and A is symmetric with a zero diagonal and no negative weight, the
+// iteration's fixed point is the all-pairs shortest-path matrix A*, and
+// H <- H (x) H reaches it in ceil(log2(hop diameter)) products instead of
+// one step per hop (H_t = A^(2^t); once a product changes nothing, every
+// higher power is equal). The same step kernel does the product with the
+// iterate as both operands. A squared entry sums two partial paths, where a
+// Jacobi step adds one edge to a path, so on float weights the roundings can
+// differ from the reference's in the last bits. On integer-valued weights
+// whose path sums stay below 2^24 every sum is exact in float, and squaring
+// gives the reference's fixed point bit for bit; the automatic mode squares
+// only then (analyze_kernel checks A on the device) and runs Jacobi steps
+// otherwise.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <cstring>
 #include <vector>
 
 #include "apsp.h"
@@ -138,6 +154,33 @@ hedetniemi_step_kernel(const float* __restrict__ X, const float* __restrict__ Ap
         }
     }
     if (__syncthreads_or(diff) && tid == 0) changed[step] = 1;
+}
+
+// Properties of A that decide whether repeated squaring applies:
+// flags bit 0 asymmetric, bit 1 non-zero diagonal, bit 2 a negative weight or
+// NaN, bit 3 a finite weight that is not an integer; *wmax = the largest
+// finite weight (as non-negative float bits, so integer max orders them).
+__global__ void analyze_kernel(const float* __restrict__ A, int n, int* flags, int* wmax) {
+    int f = 0, w = 0;
+    const size_t nn = (size_t)n * n;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < nn;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int i = static_cast<int>(idx / n), j = static_cast<int>(idx % n);
+        const float a = __ldg(A + idx);
+        if (__float_as_int(a) != __float_as_int(__ldg(A + (size_t)j * n + i))) f |= 1;
+        if (i == j && a != 0.f) f |= 2;
+        if (!(a >= 0.f)) f |= 4;
+        if (a >= 0.f && a < __int_as_float(0x7f800000)) {
+            if (a != rintf(a)) f |= 8;
+            w = max(w, __float_as_int(a));
+        }
+    }
+    f = __reduce_or_sync(0xffffffffu, f);
+    w = __reduce_max_sync(0xffffffffu, w);
+    if ((threadIdx.x & 31) == 0) {
+        if (f) atomicOr(flags, f);
+        atomicMax(wmax, w);
+    }
 }
 
 // dst (P x P) = src (n x n, stride n) or its transpose, +inf outside n x n.
@@ -269,7 +312,36 @@ struct Iterates {
     }
 };
 
+std::atomic<int> g_method{-1};
+
+// Whether repeated squaring gives this solve's result (see the file comment).
+bool use_squaring(const float* A, int n, int max_path_length, cudaStream_t s) {
+    const int method = g_method.load();
+    if (method == 0 || n < 2 || max_path_length < n - 1) return false;
+    DevMem info(2 * sizeof(int), s);
+    int* d = static_cast<int*>(info.p);
+    NSG_CUDA(cudaMemsetAsync(d, 0, 2 * sizeof(int), s));
+    const size_t nn = (size_t)n * n;
+    const int blocks = static_cast<int>(std::min<size_t>((nn + 255) / 256, 4096));
+    analyze_kernel<<<blocks, 256, 0, s>>>(A, n, d, d + 1);
+    NSG_CUDA(cudaGetLastError());
+    int h[2] = {0, 0};
+    NSG_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+    NSG_CUDA(cudaStreamSynchronize(s));
+    if (h[0] & 7) return false;            // asymmetric, diagonal, negative or NaN
+    if (method == 1) return true;          // squaring requested on any weights
+    float wmax;
+    std::memcpy(&wmax, &h[1], sizeof(float));
+    // integer weights with every path sum (at most n-1 edges) exact in float
+    return !(h[0] & 8) && static_cast<double>(wmax) * (n - 1) < 16777216.0;
+}
+
 }  // namespace
+
+void apsp_set_method(int method) {
+    if (method < -1 || method > 1) invalid("method must be -1, 0 or 1");
+    g_method.store(method);
+}
 
 int apsp_lengths(const float* A, float* H, int n, int max_path_length, cudaStream_t s) {
     if (n < 0 || max_path_length < 0) invalid("negative size or path length");
@@ -277,6 +349,31 @@ int apsp_lengths(const float* A, float* H, int n, int max_path_length, cudaStrea
     if (max_path_length == 0 || n == 0) {
         NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
         return 0;
+    }
+    if (use_squaring(A, n, max_path_length, s)) {
+        // A symmetric: X = A^T = A; each product X <- X (x) X
+        Iterates it(A, n, s);
+        int log2n = 0;
+        while ((1 << log2n) < n) ++log2n;
+        const int cap = log2n + 2;  // powers up to 2^t >= n - 1, then the unchanged product
+        DevMem changed(sizeof(int) * cap, s);
+        NSG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int) * cap, s));
+        int* ch = static_cast<int*>(changed.p);
+        for (int t = 0; t < cap; ++t) launch_step(it.X[t & 1], it.X[t & 1], it.X[(t + 1) & 1], n, it.P, ch, t, s);
+        std::vector<int> flags(cap);
+        NSG_CUDA(cudaMemcpyAsync(flags.data(), ch, sizeof(int) * cap, cudaMemcpyDeviceToHost, s));
+        NSG_CUDA(cudaStreamSynchronize(s));
+        int products = cap;
+        for (int q = 0; q < cap; ++q) {
+            if (flags[q] == 0) {
+                products = q + 1;
+                break;
+            }
+        }
+        if (products == cap && flags[cap - 1]) fail(NSG_ERR_CUDA, "shortest-path squaring did not converge");
+        launch_unpad(it.X[cap & 1], H, n, it.P, s);
+        NSG_CUDA(cudaStreamSynchronize(s));
+        return products;
     }
     Iterates it(A, n, s);
     DevMem changed(sizeof(int) * max_path_length, s);

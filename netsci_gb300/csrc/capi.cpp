@@ -506,10 +506,19 @@ int nsg_ksg_plan_search(const nsg_ksg_plan* plan, int* mode) {
 }
 
 int nsg_ksg_plan_evaluations(const nsg_ksg_plan* plan, unsigned long long* search,
-                             unsigned long long* counts) {
+                             unsigned long long* counts, unsigned long long* compares) {
     return guarded([&] {
         if (!plan || !plan->plan) nsg::invalid("plan is null");
-        plan->plan->evaluations(search, counts);
+        if (!search || !counts) nsg::invalid("null output");
+        plan->plan->evaluations(search, counts, compares);
+    });
+}
+
+int nsg_ksg_plan_kernel_ms(const nsg_ksg_plan* plan, float* search_ms, float* count_ms) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        if (!search_ms || !count_ms) nsg::invalid("null output");
+        plan->plan->kernel_ms(search_ms, count_ms);
     });
 }
 
@@ -567,11 +576,22 @@ int nsg_ksg_set_search(int mode) {
     });
 }
 
+int nsg_measure_issue_ceiling(int d, double* search_gops, double* count_gops) {
+    return guarded([&] {
+        if (!search_gops || !count_gops) nsg::invalid("null output");
+        nsg::measure_issue_ceiling(d, search_gops, count_gops);
+    });
+}
+
 int nsg_ksg_set_orders(int mode) {
     return guarded([&] {
         if (mode < -1 || mode > 1) nsg::invalid("orders must be -1, 0 or 1");
         nsg::ksg_force_orders(mode);
     });
+}
+
+int nsg_apsp_set_method(int method) {
+    return guarded([&] { nsg::apsp_set_method(method); });
 }
 
 int nsg_apsp_lengths_device(const float* A, float* H, int n, int L, int* steps, void* stream) {

@@ -267,6 +267,10 @@ long long count_items(const std::vector<nsg_ksg_pair>& pairs, int qc) {
 
 }  // namespace
 
+// Timing events per batch: search begin, search end, counts begin (after
+// the count-order kernel), counts end.
+constexpr int kEventsPerBatch = 4;
+
 KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const KsgOutputs& out,
                  const KsgPlanOptions& opt)
     : d_(d), k_(k), kmax_(ksg_kmax_for(k)), timing_(opt.timing), out_(out), graph_(opt.graph) {
@@ -533,7 +537,7 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const 
         if (search_) setup_grid(descs);
     }
     if (timing_) {
-        events_.resize(2 * batches_.size());
+        events_.resize(kEventsPerBatch * batches_.size());
         for (auto& e : events_) NSG_CUDA(cudaEventCreate(&e));
     }
 }
@@ -572,10 +576,15 @@ void KsgPlan::enqueue(cudaStream_t s) {
         a.eps_y = out_.eps_y;
         a.kdist = out_.kdist;
         // Under capture, external records stay real event nodes in the graph.
-        if (timing_) record_event(events_[2 * bi], s);
+        // The exhaustive kernel runs both passes: it is the search interval,
+        // and the count interval is empty.
+        cudaEvent_t* ev = events_.data() + kEventsPerBatch * bi;
+        if (timing_) record_event(ev[0], s);
         entry_->launch(a, b.grid, s);
         NSG_CUDA(cudaGetLastError());
-        if (timing_) record_event(events_[2 * bi + 1], s);
+        if (timing_) {
+            for (int j = 1; j < kEventsPerBatch; ++j) record_event(ev[j], s);
+        }
         KsgTieArgs t{};
         t.pairs = pairs_dev_.as<KsgPairDesc>();
         t.ties = ties_.as<KsgTie>();
@@ -622,7 +631,7 @@ struct KsgPlan::GridState {
     std::vector<int> ngroups;
     DeviceBuffer corder;                  // count-query order: ngroups x largest m of a batch
     DeviceBuffer eps_a, eps_b, cnt_a, cnt_b;
-    DeviceBuffer evals;                   // 2 counters per run (search, counts)
+    DeviceBuffer evals;                   // 3 counters per run (see GridArgs::evals)
     int nnodes = 0;
     int search_grid = 0, count_grid = 0;
 };
@@ -736,7 +745,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
     g->eps_b.reset(ns * sizeof(float));
     g->cnt_a.reset(ns * sizeof(int));
     g->cnt_b.reset(ns * sizeof(int));
-    g->evals.reset(2 * sizeof(unsigned long long));
+    g->evals.reset(3 * sizeof(unsigned long long));
     g->search_grid = sm_count() * grid_search_ctas_per_sm(d_, kmax_);
     g->count_grid = sm_count() * grid_count_ctas_per_sm(d_);
     grid_ = std::move(g);
@@ -746,7 +755,7 @@ void KsgPlan::setup_grid(const std::vector<KsgPairDesc>& descs) {
 
 void KsgPlan::enqueue_grid(cudaStream_t s) {
     GridState& g = *grid_;
-    NSG_CUDA(cudaMemsetAsync(g.evals.get(), 0, 2 * sizeof(unsigned long long), s));
+    NSG_CUDA(cudaMemsetAsync(g.evals.get(), 0, 3 * sizeof(unsigned long long), s));
     grid_launch_gather(gather_rows_.as<GatherRow>(), ngather_, d_, fault_.as<int>(), s);
     grid_launch_nodes(g.nodes.as<GridNode>(), g.nnodes, d_, g.node_est, s);
     for (size_t bi = 0; bi < batches_.size(); ++bi) {
@@ -784,11 +793,15 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         a.kdist = out_.kdist;
         a.corder = order ? g.corder.as<int>() : nullptr;
         a.corder_ld = g.batch_maxm[bi];
-        if (timing_) record_event(events_[2 * bi], s);
+        cudaEvent_t* ev = events_.data() + kEventsPerBatch * bi;
+        if (timing_) record_event(ev[0], s);
         grid_launch_search(a, d_, kmax_, g.search_grid, s);
+        if (timing_) record_event(ev[1], s);
         a.counter = ctr + 1;
-        grid_launch_counts(a, d_, g.count_grid, s);
-        if (timing_) record_event(events_[2 * bi + 1], s);
+        const GridArgs c = grid_launch_count_order(a, s);
+        if (timing_) record_event(ev[2], s);
+        grid_launch_count_kernel(c, d_, g.count_grid, s);
+        if (timing_) record_event(ev[3], s);
         grid_launch_combine(bp, b.npairs, g.cnt_a.as<int>(), g.cnt_b.as<int>(), psi_->as<float>(),
                             scratch_.as<float>(), out_.nx, out_.ny, s);
         KsgTieArgs t{};
@@ -841,13 +854,16 @@ int KsgPlan::launches() const {
 
 int KsgPlan::staging() const { return entry_ ? entry_->tma : 0; }
 
-void KsgPlan::evaluations(unsigned long long* search, unsigned long long* counts) const {
+void KsgPlan::evaluations(unsigned long long* search, unsigned long long* counts,
+                          unsigned long long* compares) const {
     *search = *counts = 0;
+    if (compares) *compares = 0;
     if (!search_ || !grid_) return;
-    unsigned long long h[2] = {0, 0};
+    unsigned long long h[3] = {0, 0, 0};
     NSG_CUDA(cudaMemcpy(h, grid_->evals.get(), sizeof(h), cudaMemcpyDeviceToHost));
     *search = h[0];
     *counts = h[1];
+    if (compares) *compares = h[2];
 }
 
 int KsgPlan::take_fault() {
@@ -953,15 +969,25 @@ KsgTuned ksg_autotune(const std::vector<nsg_ksg_pair>& pairs, int k, int d) {
 }
 
 float KsgPlan::count_ms() const {
+    float search = 0.f, counts = 0.f;
+    kernel_ms(&search, &counts);
+    return search + counts;
+}
+
+void KsgPlan::kernel_ms(float* search_ms, float* count_ms) const {
     if (!timing_) fail(NSG_ERR_INVALID, "plan was created without timing events");
-    float total = 0.f;
+    float search = 0.f, counts = 0.f;
     for (size_t b = 0; b < batches_.size(); ++b) {
-        NSG_CUDA(cudaEventSynchronize(events_[2 * b + 1]));
+        const cudaEvent_t* ev = events_.data() + kEventsPerBatch * b;
+        NSG_CUDA(cudaEventSynchronize(ev[3]));
         float ms = 0.f;
-        NSG_CUDA(cudaEventElapsedTime(&ms, events_[2 * b], events_[2 * b + 1]));
-        total += ms;
+        NSG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        search += ms;
+        NSG_CUDA(cudaEventElapsedTime(&ms, ev[2], ev[3]));
+        counts += ms;
     }
-    return total;
+    *search_ms = search;
+    *count_ms = counts;
 }
 
 void KsgPlan::run(cudaStream_t s) {

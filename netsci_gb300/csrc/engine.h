@@ -88,10 +88,16 @@ public:
     int variant() const { return variant_; }
     int staging() const;  // 1: bulk-copy staged kernel, 0: plain loads
     int search() const { return search_; }  // 1: cell grids, 0: exhaustive
-    // Query-frame distance evaluations of the last run's grid search (joint
-    // distances) and grid counts (one variable's distance); 0 when exhaustive.
+    // Query-frame evaluations of the last run's grid search (joint
+    // distances), grid counts (one variable's distance, once per query and
+    // frame) and the counts' eps comparisons (once per query, frame and pair
+    // of a count group); 0 when exhaustive. compares may be null.
     // Synchronizes with the device.
-    void evaluations(unsigned long long* search, unsigned long long* counts) const;
+    void evaluations(unsigned long long* search, unsigned long long* counts,
+                     unsigned long long* compares = nullptr) const;
+    // Device milliseconds of the last run's search kernels and count kernels
+    // (the order kernels excluded), summed over batches; needs timing.
+    void kernel_ms(float* search_ms, float* count_ms) const;
 
 private:
     struct Batch {
@@ -159,5 +165,8 @@ int ksg_forced_orders();
 // plane stride a multiple of 4, no frame map).
 bool ksg_bulk_copy_ok(const std::vector<nsg_ksg_pair>& pairs);
 int sm_count();
+// Operation rates (Gop/s) of the cell-grid search and count kernels' inner
+// loops alone, measured on the current device (ceiling.cu).
+void measure_issue_ceiling(int d, double* search_gops, double* count_gops);
 
 }  // namespace nsg

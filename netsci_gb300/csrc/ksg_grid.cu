@@ -644,7 +644,7 @@ void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream
     NSG_CUDA(cudaGetLastError());
 }
 
-void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st) {
+GridArgs grid_launch_count_order(const GridArgs& a, cudaStream_t st) {
     GridArgs c = a;
     if (c.corder && c.corder_ld <= kOrderMaxM && c.ngroups > 0) {
         const size_t smem = sizeof(unsigned) * static_cast<size_t>(c.corder_ld);
@@ -656,6 +656,10 @@ void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st) {
     } else {
         c.corder = nullptr;
     }
+    return c;
+}
+
+void grid_launch_count_kernel(const GridArgs& c, int d, int grid, cudaStream_t st) {
     const dim3 b(32 * kGridWarps);
     switch (d) {
         case 1: ksg_grid_count_kernel<1><<<grid, b, 0, st>>>(c); break;
@@ -664,6 +668,10 @@ void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st) {
         default: invalid("d must be 1, 2 or 3");
     }
     NSG_CUDA(cudaGetLastError());
+}
+
+void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st) {
+    grid_launch_count_kernel(grid_launch_count_order(a, st), d, grid, st);
 }
 
 void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a, const int* cnt_b,

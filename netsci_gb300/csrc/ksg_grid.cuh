@@ -577,8 +577,11 @@ __global__ void __launch_bounds__(32 * kGridWarps, 4) ksg_grid_count_kernel(Grid
                 if (p < grp.npairs) out[A.pairs[grp.pairs[p]].scratch + i] = cnt[p];
         }
         if (A.evals && lane == 0) {
-            atomicAdd(A.evals + 1, static_cast<unsigned long long>(scanned) *
-                                       min(kCountQueries, m - blk * kCountQueries) * grp.npairs);
+            // one distance per (query, frame), compared with every pair's eps
+            const unsigned long long ev =
+                static_cast<unsigned long long>(scanned) * min(kCountQueries, m - blk * kCountQueries);
+            atomicAdd(A.evals + 1, ev);
+            atomicAdd(A.evals + 2, ev * grp.npairs);
         }
     }
 }

@@ -89,7 +89,10 @@ struct GridArgs {
     float* eps_b;
     int* cnt_a;
     int* cnt_b;
-    // lane-frame distance evaluations done: [0] search, [1] counts
+    // query-frame evaluations done: [0] joint distances of the search,
+    // [1] one-variable distances of the counts (one per query and frame,
+    // shared by the group's pairs), [2] the counts' eps comparisons (one per
+    // query, frame and pair of the group)
     unsigned long long* evals;
     // optional per-sample outputs
     float* eps_x;
@@ -155,6 +158,11 @@ int grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* n
                       int max_m, int d, bool order, cudaStream_t st);
 void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st);
 void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st);
+// The two halves of grid_launch_counts: the count-order kernel (when the
+// args carry a count order; returns the args the count kernel takes), then
+// the count kernel itself.
+GridArgs grid_launch_count_order(const GridArgs& a, cudaStream_t st);
+void grid_launch_count_kernel(const GridArgs& c, int d, int grid, cudaStream_t st);
 void grid_launch_combine(const KsgPairDesc* pairs, int npairs, const int* cnt_a, const int* cnt_b,
                          const float* psi, float* psum, int* nx, int* ny, cudaStream_t st);
 // Copies frame-mapped rows (device array of nrows); a map entry outside

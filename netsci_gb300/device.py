@@ -133,12 +133,22 @@ class KsgPlan:
                     staging="bulk-copy" if v[4].value else "loads",
                     search="cell-grid" if v[5].value else "exhaustive")
 
-    def evaluations(self) -> tuple[int, int]:
-        """(joint-distance, one-variable-distance) query-frame evaluations of
-        the last run's cell-grid search; (0, 0) for exhaustive plans."""
-        a, b = ctypes.c_ulonglong(), ctypes.c_ulonglong()
-        call("nsg_ksg_plan_evaluations", self._h, ctypes.byref(a), ctypes.byref(b))
-        return a.value, b.value
+    def evaluations(self) -> tuple[int, int, int]:
+        """(joint distances, one-variable distances, eps comparisons) of the
+        last run's cell-grid search and counts; zeros for exhaustive plans.
+        A count kernel's distance is evaluated once per query and frame and
+        compared with the eps of every pair of its count group."""
+        a, b, c = ctypes.c_ulonglong(), ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        call("nsg_ksg_plan_evaluations", self._h, ctypes.byref(a), ctypes.byref(b),
+             ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def kernel_ms(self) -> tuple[float, float]:
+        """Device ms of the last run's (search, count) kernels, order kernels
+        excluded; plans need timing=True."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        call("nsg_ksg_plan_kernel_ms", self._h, ctypes.byref(a), ctypes.byref(b))
+        return float(a.value), float(b.value)
 
     def count_ms(self) -> float:
         """Device time (ms) of the count kernels in the last run."""
@@ -181,6 +191,20 @@ def set_ksg_search(mode: int = -1) -> None:
 def set_ksg_orders(mode: int = -1) -> None:
     """Block query orders of later cell-grid plans: 1 always, 0 never, -1 automatic."""
     call("nsg_ksg_set_orders", int(mode))
+
+
+def issue_ceiling(d: int = 3) -> tuple[float, float]:
+    """Measured operation rates (Gop/s) of the cell-grid search and count
+    kernels' inner loops alone: the ceilings their rates are divided by."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    call("nsg_measure_issue_ceiling", int(d), ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+def set_apsp_method(method: int = -1) -> None:
+    """Shortest-path products for later solves: -1 automatic (squaring where
+    bit-exact), 0 Jacobi steps only, 1 squaring on any weights."""
+    call("nsg_apsp_set_method", int(method))
 
 
 def apsp_lengths(A: torch.Tensor, max_path_length: int, H: torch.Tensor | None = None,

@@ -5,7 +5,10 @@ of the per-rank times (weak scaling: value = pairs of all ranks / slowest
 rank's time).
 
 Batch s of rank r covers pairs [(r*S + s)*B, (r*S + s + 1)*B) of the pair
-list, S = steps per rank (warm-up included), B = pairs per step.
+list, S = steps per rank (warm-up included), B = pairs per step
+(``rank_batch``); ``spread_batch`` places the world*S batches evenly over
+the whole list instead, so that a sample of steps covers every part of the
+all-pairs job (its pairs' rows a run from 0 to N-2).
 """
 from __future__ import annotations
 
@@ -15,6 +18,18 @@ import numpy as np
 def rank_batch(ab: np.ndarray, rank: int, steps: int, step: int, per_step: int) -> np.ndarray:
     """Pairs of batch `step` of `rank` (a view into `ab`)."""
     off = (rank * steps + step) * per_step
+    return ab[off:off + per_step]
+
+
+def spread_batch(ab: np.ndarray, rank: int, world: int, steps: int, step: int,
+                 per_step: int) -> np.ndarray:
+    """Batch `step` of `rank` when the world*steps batches of per_step
+    consecutive pairs are spread evenly over the pair list (first batch at
+    the start, last at the end; disjoint while world*steps*per_step <= len)."""
+    g = rank * steps + step
+    n = world * steps
+    span = max(0, len(ab) - per_step)
+    off = 0 if n <= 1 else span * g // (n - 1)
     return ab[off:off + per_step]
 
 

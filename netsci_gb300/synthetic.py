@@ -102,11 +102,13 @@ def contact_graph(mean: np.ndarray, gc_pairs: np.ndarray, ab: np.ndarray,
     N = mean.shape[0]
     A = np.full((N, N), np.float32(np.inf), dtype=np.float32)
     dist = np.linalg.norm(mean[:, None, :] - mean[None, :, :], axis=-1)
-    for (a, b), g in zip(ab, gc_pairs):
-        if dist[a, b] < cutoff and g > 0:
-            w = np.float32(-np.log(np.float64(g)))
-            A[a, b] = w
-            A[b, a] = w
+    ab = np.asarray(ab, dtype=np.int64).reshape(-1, 2)
+    g = np.asarray(gc_pairs, dtype=np.float32)
+    a, b = ab[:, 0], ab[:, 1]
+    keep = (dist[a, b] < cutoff) & (g > 0)
+    w = (-np.log(g[keep].astype(np.float64))).astype(np.float32)
+    A[a[keep], b[keep]] = w
+    A[b[keep], a[keep]] = w
     np.fill_diagonal(A, 0.0)
     return A
 

@@ -3,7 +3,10 @@
 Bar: lengths bit-exact against the oracle's Jacobi iteration for float and
 integer weights (each entry is a minimum of single roundings, independent
 of evaluation order), and equal to Floyd-Warshall on integer weights;
-paths bit-exact against the oracle's walk.
+paths bit-exact against the oracle's walk. Where repeated squaring applies
+(the fixed point of a symmetric, zero-diagonal, non-negative graph) it is
+bit-exact on integer weights and, when forced on float weights, within
+1e-6 relative of the Jacobi fixed point.
 """
 import numpy as np
 import pytest
@@ -24,15 +27,62 @@ def test_protein56_contact_graph_lengths(golden):
     assert np.array_equal(H.cpu().numpy(), z["H"])
 
 
+@pytest.fixture
+def apsp_method():
+    from netsci_gb300 import device
+    yield device.set_apsp_method
+    device.set_apsp_method(-1)
+
+
 @pytest.mark.parametrize("n", [1, 7, 128, 300, 257])
-def test_integer_rgg_matches_floyd_warshall(oracle_mod, n):
+def test_integer_rgg_matches_floyd_warshall(oracle_mod, apsp_method, n):
+    """Automatic schedule (repeated squaring on these graphs) and Jacobi
+    steps: both equal Floyd-Warshall; Jacobi takes the oracle's step count,
+    squaring about log2 of it."""
     from netsci_gb300 import device, synthetic
     A = synthetic.random_geometric_graph(n, 8, seed=n, integer_weights=True)
-    H, steps = device.apsp_lengths(_dev(A), n)
     D = oracle_mod.floyd_warshall(A)
-    assert np.array_equal(H.cpu().numpy(), D)
     Ho, so, conv = oracle_mod.apsp_lengths(A, n)
+    H, products = device.apsp_lengths(_dev(A), n)
+    assert np.array_equal(H.cpu().numpy(), D)
+    if n > 1:
+        # Jacobi's count is the hop diameter h; squaring runs ceil(log2 h)
+        # products to reach it and one more that changes nothing
+        assert products == int(np.ceil(np.log2(so))) + 1
+    apsp_method(0)
+    H, steps = device.apsp_lengths(_dev(A), n)
+    assert np.array_equal(H.cpu().numpy(), D)
     assert steps == so
+
+
+def test_squaring_schedule_rules(oracle_mod, apsp_method):
+    """Squaring only where it reaches the Jacobi fixed point: asymmetric,
+    truncated (maxPathLength < n-1) or non-integer inputs take Jacobi steps
+    in the automatic mode (the step count tells which schedule ran)."""
+    from netsci_gb300 import device, synthetic
+    n = 200
+    A = synthetic.random_geometric_graph(n, 5, seed=9, integer_weights=True)
+    Ho, so, _ = oracle_mod.apsp_lengths(A, n)
+    assert so > 8
+    _, p = device.apsp_lengths(_dev(A), n)
+    assert p < so
+    _, p = device.apsp_lengths(_dev(A), n - 2)     # truncated: Jacobi
+    assert p == min(so, n - 2)
+    B = A.copy()
+    B[3, 7] = B[7, 3] + 1 if np.isfinite(B[7, 3]) else 5.0   # asymmetric: Jacobi
+    Hb, pb = device.apsp_lengths(_dev(B), n)
+    Hob, sob, _ = oracle_mod.apsp_lengths(B, n)
+    assert pb == sob and np.array_equal(Hb.cpu().numpy(), Hob)
+    C = A.copy()
+    C[np.isfinite(C) & (C > 0)] += 0.5                         # non-integer: Jacobi
+    Hc, pc = device.apsp_lengths(_dev(C), n)
+    Hoc, soc, _ = oracle_mod.apsp_lengths(C, n)
+    assert pc == soc and np.array_equal(Hc.cpu().numpy(), Hoc)
+    # forced squaring on float weights: within 1e-6 relative of Jacobi
+    apsp_method(1)
+    Hf, pf = device.apsp_lengths(_dev(C), n)
+    assert pf < soc
+    np.testing.assert_allclose(Hf.cpu().numpy(), Hoc, rtol=1e-6)
 
 
 @pytest.mark.parametrize("n", [200, 383])

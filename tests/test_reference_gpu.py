@@ -30,21 +30,32 @@ def ref_gpu(oracle_mod):
     return oracle_mod
 
 
-def _ours(A, L):
+def _ours(A, L, method=-1):
     from netsci_gb300 import device
-    H, steps = device.apsp_lengths(torch.from_numpy(np.ascontiguousarray(A, np.float32)).cuda(), L)
+    device.set_apsp_method(method)
+    try:
+        H, steps = device.apsp_lengths(torch.from_numpy(np.ascontiguousarray(A, np.float32)).cuda(), L)
+    finally:
+        device.set_apsp_method(-1)
     return H.cpu().numpy(), steps
 
 
 @pytest.mark.parametrize("n,degree,integer", [(2000, 12, True), (2000, 12, False), (300, 6, True),
                                               (257, 8, False), (64, 3, True)])
 def test_apsp_fixed_point_equals_reference_kernel(ref_gpu, n, degree, integer):
+    """Jacobi steps and the automatic schedule (repeated squaring on the
+    integer graphs) both give the reference kernel's fixed point; the
+    reference runs the Jacobi step count plus two launches."""
     from netsci_gb300 import synthetic
     A = synthetic.random_geometric_graph(n, degree, seed=11 if n == 2000 else n,
                                          integer_weights=integer)
-    H, steps = _ours(A, n)
+    Hj, steps = _ours(A, n, method=0)
     Href = ref_gpu.ref_gpu_apsp_lengths(A, steps + 2)
+    assert np.array_equal(Hj, Href)
+    H, products = _ours(A, n)
     assert np.array_equal(H, Href)
+    if integer and n > 64:
+        assert products < steps
 
 
 def test_apsp_protein56_contact_graph_equals_reference_kernel(ref_gpu, golden):
