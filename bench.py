@@ -755,17 +755,31 @@ def main():
 
     # ---- other configurations (rank 0) ----------------------------------------------
     extra = {}
+
+    def section(name, fn):
+        """Run one secondary measurement; a failure is reported in the line
+        (with its message) instead of losing the headline numbers."""
+        try:
+            return fn()
+        except Exception as e:  # noqa: BLE001
+            torch.cuda.synchronize()
+            return {"error": f"{type(e).__name__}: {e}"}
+
     if rank == 0:
         if not args.no_c4_full and not args.quick:
-            full, A_c4, H_c4, steps_c4 = c4_full(X, mean, m, ab_all)
-            extra["c4_full"] = full
-            apsp_graphs["c4_neglog_gc"] = (A_c4, H_c4, steps_c4)
+            def run_c4():
+                full, A_c4, H_c4, steps_c4 = c4_full(X, mean, m, ab_all)
+                apsp_graphs["c4_neglog_gc"] = (A_c4, H_c4, steps_c4)
+                return full
+            extra["c4_full"] = section("c4_full", run_c4)
         if args.c3_trajectories:
-            extra["uneven_batch"] = uneven_batch(args.c3_trajectories, args.quick)
+            extra["uneven_batch"] = section("uneven_batch",
+                                            lambda: uneven_batch(args.c3_trajectories, args.quick))
         if args.bootstrap_resamples:
-            extra["bootstrap"] = bootstrap(X, m, args.bootstrap_resamples)
+            extra["bootstrap"] = section("bootstrap",
+                                         lambda: bootstrap(X, m, args.bootstrap_resamples))
         if args.serving_requests:
-            extra["serving"] = serving(args.serving_requests, args.quick)
+            extra["serving"] = section("serving", lambda: serving(args.serving_requests, args.quick))
 
     # ---- CPU baseline and parity: the reference's CPU code on pairs of the timed steps --
     cpu = parity = None
@@ -797,7 +811,7 @@ def main():
     if rank == 0 and not args.no_reference_gpu and not args.quick:
         pool = timed_pair_pool(ab_all, world, S, args.warmup, B)
         sel = pool[np.random.default_rng(4).choice(len(pool), size=5, replace=False)]
-        ref_gpu = reference_gpu(X, m, sel, apsp_graphs)
+        ref_gpu = section("reference_gpu", lambda: reference_gpu(X, m, sel, apsp_graphs))
 
     if rank == 0:
         line = {

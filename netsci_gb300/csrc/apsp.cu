@@ -314,10 +314,12 @@ struct Iterates {
 
 std::atomic<int> g_method{-1};
 
-// Whether repeated squaring gives this solve's result (see the file comment).
-bool use_squaring(const float* A, int n, int max_path_length, cudaStream_t s) {
+// Whether repeated squaring gives this solve's result (see the file comment):
+// 0 no, 1 exactly (integer weights), 2 within rounding (requested on float
+// weights).
+int use_squaring(const float* A, int n, int max_path_length, cudaStream_t s) {
     const int method = g_method.load();
-    if (method == 0 || n < 2 || max_path_length < n - 1) return false;
+    if (method == 0 || n < 2 || max_path_length < n - 1) return 0;
     DevMem info(2 * sizeof(int), s);
     int* d = static_cast<int*>(info.p);
     NSG_CUDA(cudaMemsetAsync(d, 0, 2 * sizeof(int), s));
@@ -328,12 +330,12 @@ bool use_squaring(const float* A, int n, int max_path_length, cudaStream_t s) {
     int h[2] = {0, 0};
     NSG_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
     NSG_CUDA(cudaStreamSynchronize(s));
-    if (h[0] & 7) return false;            // asymmetric, diagonal, negative or NaN
-    if (method == 1) return true;          // squaring requested on any weights
+    if (h[0] & 7) return 0;                // asymmetric, diagonal, negative or NaN
     float wmax;
     std::memcpy(&wmax, &h[1], sizeof(float));
     // integer weights with every path sum (at most n-1 edges) exact in float
-    return !(h[0] & 8) && static_cast<double>(wmax) * (n - 1) < 16777216.0;
+    if (!(h[0] & 8) && static_cast<double>(wmax) * (n - 1) < 16777216.0) return 1;
+    return method == 1 ? 2 : 0;            // squaring requested on any weights
 }
 
 }  // namespace
@@ -350,12 +352,17 @@ int apsp_lengths(const float* A, float* H, int n, int max_path_length, cudaStrea
         NSG_CUDA(cudaMemcpyAsync(H, A, nn * sizeof(float), cudaMemcpyDeviceToDevice, s));
         return 0;
     }
-    if (use_squaring(A, n, max_path_length, s)) {
+    if (const int sq = use_squaring(A, n, max_path_length, s)) {
         // A symmetric: X = A^T = A; each product X <- X (x) X
         Iterates it(A, n, s);
         int log2n = 0;
         while ((1 << log2n) < n) ++log2n;
-        const int cap = log2n + 2;  // powers up to 2^t >= n - 1, then the unchanged product
+        // Exact sums: powers up to 2^t >= n - 1, then the product that changes
+        // nothing. Rounded sums: once every shortest path is covered, a product
+        // can still lower an entry by an ulp through another split of a path's
+        // sum; those descents are bounded and short, and products that find
+        // nothing to change return at once.
+        const int cap = sq == 1 ? log2n + 2 : log2n + 64;
         DevMem changed(sizeof(int) * cap, s);
         NSG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int) * cap, s));
         int* ch = static_cast<int*>(changed.p);

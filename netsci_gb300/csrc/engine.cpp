@@ -515,18 +515,16 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const 
         // per batch: work-queue head, tie count, tie-kernel work counter
         counters_.reset(kCounters * batches_.size() * sizeof(int));
         // Samples with an ambiguous tie are rare (about 1e-4 on trajectory
-        // data; ties among copies of one frame are not listed); the list
-        // holds a quarter of the largest batch's samples.
+        // data), but nothing bounds them: the list holds every sample of the
+        // largest batch, so it cannot overflow (8 bytes per sample, beside
+        // the 4 bytes per sample of the psi terms).
         long long batch_samples = 0;
         for (const Batch& b : batches_) {
             long long sum = 0;
             for (int p = b.pair0; p < b.pair0 + b.npairs; ++p) sum += descs[p].m;
             batch_samples = std::max(batch_samples, sum);
         }
-        // copies of resampled frames tie on many samples; on cell grids they
-        // are all listed (the tie kernel sets the harmless ones aside)
-        tie_cap_ = static_cast<int>(std::min<long long>(
-            std::max<long long>(65536, bootstrap_ ? batch_samples : batch_samples / 4), 1LL << 30));
+        tie_cap_ = static_cast<int>(std::min<long long>(std::max<long long>(1, batch_samples), 1LL << 30));
         ties_.reset(static_cast<size_t>(tie_cap_) * sizeof(KsgTie));
         tie_stride_ = maxm;
         tie_dz_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(float));

@@ -35,8 +35,9 @@ enum DeviceFault : int {
     FAULT_NONE = 0,
     FAULT_WAIT_TIMEOUT = 1,
     FAULT_BAD_INDEX = 2,
-    FAULT_TIE_OVERFLOW = 4,     // more tied samples than the tie list holds
-    FAULT_TIE_UNRESOLVED = 8,   // the sort-order replay ran out of depth budget
+    FAULT_TIE_OVERFLOW = 4,     // more tied samples than the tie list holds (lists are
+                                // sized for every sample: a broken invariant)
+    FAULT_TIE_UNRESOLVED = 8,   // the sort-order replay met a broken invariant
 };
 
 // Throws NSG_ERR_DEVICE_FAULT describing a non-zero device fault word.
@@ -46,7 +47,7 @@ inline void raise_fault(int f) {
     if (f & FAULT_WAIT_TIMEOUT) m += " a bounded wait ran out;";
     if (f & FAULT_BAD_INDEX) m += " a frame map entry is outside [0, ld);";
     if (f & FAULT_TIE_OVERFLOW) m += " more tied samples than the tie list holds;";
-    if (f & FAULT_TIE_UNRESOLVED) m += " a tied sample's sort replay ran out of depth budget;";
+    if (f & FAULT_TIE_UNRESOLVED) m += " a tied sample's sort replay met a broken invariant;";
     fail(NSG_ERR_DEVICE_FAULT, m);
 }
 

@@ -63,7 +63,9 @@ __device__ __forceinline__ float tie_marginal(const float (&q)[D], const float* 
 // stoppers can be read from the array as it was. The cut is the first left
 // stopper past the last swap, or that swap's right position if it comes
 // first. Lane 0 holds the segment stack and does the swaps; all lanes load
-// and vote. Same result as the serial routine, element for element.
+// and vote. A segment whose depth budget runs out is heapsorted by lane 0
+// (heap_sort_like_reference). Same result as the serial routine, element for
+// element.
 __device__ bool sort_prefix_warp(const float* key, int* idx, int n, int T, SortSegment* stack,
                                  int cap, int lane) {
     if (n <= 1) return true;
@@ -80,7 +82,11 @@ __device__ bool sort_prefix_warp(const float* key, int* idx, int n, int T, SortS
         int last = __shfl_sync(kFull, sg.last, 0);
         int depth = __shfl_sync(kFull, sg.depth, 0);
         while (last - first > kThreshold) {
-            if (depth == 0) return false;
+            if (depth == 0) {
+                if (lane == 0) heap_sort_like_reference(key, idx + first, last - first);
+                __syncwarp();
+                break;
+            }
             --depth;
             // median of three moved to `first` (lane 0)
             if (lane == 0) {

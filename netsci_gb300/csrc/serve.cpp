@@ -101,7 +101,9 @@ Server::Server(const ServerConfig& cfg) : cfg_(cfg) {
     d_counters_.reset(sizeof(int) * 64);
     d_fault_.reset(sizeof(int));
     NSG_CUDA(cudaMemset(d_fault_.get(), 0, sizeof(int)));
-    tie_cap_ = 1 << 22;
+    // a tick holds at most cap_samples_ samples; the tie list holds them all,
+    // so it cannot overflow
+    tie_cap_ = static_cast<int>(cap_samples_);
     d_ties_.reset(sizeof(KsgTie) * tie_cap_);
     d_tie_dz_.reset(sizeof(float) * static_cast<size_t>(kServeTieWarps) * cfg.max_m);
     d_tie_idx_.reset(sizeof(int) * static_cast<size_t>(kServeTieWarps) * cfg.max_m);

@@ -21,10 +21,18 @@
 //     never cross a partition point and each final segment can be sorted on
 //     its own.
 //
+//   * a segment on which the depth budget runs out is heapsorted, as the
+//     library's partial sort with middle == last does it: a max-heap built
+//     by sifting each parent down from the last one to the root, then the
+//     root swapped with the last element of the shrinking heap and the
+//     displaced element sifted back down. A sift-down first moves the hole
+//     to a leaf along the larger children (the right child unless it is less
+//     than the left one) and then lets the element rise from there while its
+//     parent is less than it. Those steps decide where equal keys end up.
+//
 // Only segments that intersect [0, T) are followed, which makes the work
-// O(n) instead of O(n log n). If the depth budget runs out on such a segment
-// (the sort would switch to heapsort there), the routine reports failure and
-// the caller resolves the sample another way.
+// O(n) instead of O(n log n), except on a heapsorted segment (O(L log L) for
+// its L elements, only on inputs that defeat the median-of-three pivots).
 //
 // Written for both the host (tests compare it with std::sort) and the device
 // (the tie-resolution kernel runs it per tied sample).
@@ -44,6 +52,46 @@ struct SortSegment {
     int depth;
 };
 
+// Sift-down of the heap v[0..len) (max at the root, by key[v[.]]) from the
+// hole at `hole`, placing `value` (the element that was there).
+NSG_HD void heap_sift_like_reference(const float* key, int* v, int hole, int len, int value) {
+    const int top = hole;
+    int child = hole;
+    while (child < (len - 1) / 2) {
+        child = 2 * (child + 1);
+        if (key[v[child]] < key[v[child - 1]]) --child;
+        v[hole] = v[child];
+        hole = child;
+    }
+    if ((len & 1) == 0 && child == (len - 2) / 2) {
+        child = 2 * (child + 1);
+        v[hole] = v[child - 1];
+        hole = child - 1;
+    }
+    const float kv = key[value];
+    int parent = (hole - 1) / 2;
+    while (hole > top && key[v[parent]] < kv) {
+        v[hole] = v[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    v[hole] = value;
+}
+
+// Heapsort of v[0..len) in the library's steps (heap build, then pops).
+NSG_HD void heap_sort_like_reference(const float* key, int* v, int len) {
+    if (len < 2) return;
+    for (int parent = (len - 2) / 2;; --parent) {
+        heap_sift_like_reference(key, v, parent, len, v[parent]);
+        if (parent == 0) break;
+    }
+    for (int last = len - 1; last > 0; --last) {
+        const int value = v[last];
+        v[last] = v[0];
+        heap_sift_like_reference(key, v, 0, last, value);
+    }
+}
+
 // floor(log2(n)) for n >= 1
 NSG_HD int floor_log2(int n) {
     int r = 0;
@@ -56,10 +104,12 @@ NSG_HD int floor_log2(int n) {
 
 // Rearranges idx[0..n) (initially 0..n-1) as the reference sort would, at
 // least on positions [0, T). key[v] is the sort key of value v. `stack`
-// must hold at least 2*floor(log2 n) + 2 segments. Returns false when the
-// depth budget ran out on a segment covering [0, T).
+// must hold at least 2*floor(log2 n) + 2 segments. Returns false only when
+// the stack is too small or a partition invariant breaks (neither happens
+// with a large enough stack). *heapsorted (nullable) counts the segments
+// that took the heapsort branch.
 NSG_HD bool sort_prefix_like_reference(const float* key, int* idx, int n, int T,
-                                       SortSegment* stack, int stack_cap) {
+                                       SortSegment* stack, int stack_cap, int* heapsorted = nullptr) {
     if (n <= 1) return true;
     constexpr int kThreshold = 16;
     int top = 0;
@@ -73,7 +123,12 @@ NSG_HD bool sort_prefix_like_reference(const float* key, int* idx, int n, int T,
         SortSegment s = stack[--top];
         int first = s.first, last = s.last, depth = s.depth;
         while (last - first > kThreshold) {
-            if (depth == 0) return false;
+            if (depth == 0) {
+                // depth budget spent: the segment is heapsorted and final
+                heap_sort_like_reference(key, idx + first, last - first);
+                if (heapsorted) ++*heapsorted;
+                break;
+            }
             --depth;
             // median of three moved to `first`
             const int a = first + 1, b = first + (last - first) / 2, c = last - 1;

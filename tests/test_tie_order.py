@@ -20,7 +20,8 @@ def test_sort_prefix_matches_std_sort(tmp_path):
                     str(ROOT / "tests" / "native" / "sort_prefix_check.cpp"), "-o", str(exe)],
                    check=True)
     out = subprocess.run([str(exe), "6000"], capture_output=True, text=True, check=True).stdout
-    assert out.strip() == "ok 6000", out
+    assert out.startswith("ok 6000 heapsorted "), out
+    assert int(out.split()[-1]) > 0, out  # the heapsort branch was exercised
 
 
 def test_oracle_counts_ties_on_coarse_grid(oracle_mod):
