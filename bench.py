@@ -314,6 +314,7 @@ def uneven_batch(n_traj: int, quick: bool):
         apsp_steps += st
     torch.cuda.synchronize()
     apsp_s = time.perf_counter() - t0
+    shape = plan.shape
     plan.close()
     return {"trajectories": n_traj, "pairs": P, "batched_pairs_per_s": P / batched_s,
             "batched_s": batched_s, "batched_top_s": ops / batched_s / 1e12,
@@ -321,7 +322,7 @@ def uneven_batch(n_traj: int, quick: bool):
             "speedup_vs_plain": (P / batched_s) / plain_pairs_per_s,
             "plain_sample": f"{len(xs)} pairs, one netcalc.generalizedCorrelationGpu call each, "
                             "rate scaled to the batch's mean work per pair",
-            "tile": plan.shape, "apsp_total_ms": 1000 * apsp_s, "apsp_steps": apsp_steps}
+            "tile": shape, "apsp_total_ms": 1000 * apsp_s, "apsp_steps": apsp_steps}
 
 
 def c4_full(X, mean, m, ab_all):

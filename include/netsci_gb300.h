@@ -271,8 +271,11 @@ int nsg_ksg_plan_kernel_ms(const nsg_ksg_plan* plan, float* search_ms, float* co
  * NSG_NOALLOC_SCRATCH_BYTES device array inside the library, present on
  * every GPU that loads it until the process exits. The first call on each
  * device (with that device current) looks the array up and fills its psi
- * table, so make it before any stream capture. Calls share the array:
- * calls whose work overlaps on the GPU race. m is at most
+ * table, so make it before any stream capture. The address and the table
+ * are kept for the life of the process: a host that resets the device
+ * (cudaDeviceReset) after that first call cannot use this entry point any
+ * more. Calls share the array: calls whose work overlaps on the GPU race.
+ * m is at most
  * NSG_NOALLOC_MAX_SAMPLES (larger m: NSG_ERR_UNSUPPORTED). Rows as in
  * nsg_ksg_pair_detail_device; mi, gc: device float[1] each, one nullable.
  * Synchronizes `stream`.                                                  */

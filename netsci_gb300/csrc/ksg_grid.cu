@@ -343,66 +343,76 @@ __device__ __forceinline__ int block_zcode(int bx, int by) {
     return z;
 }
 
-// Sort key of a box size e >= 0 at storage position pos < 65536: the top 16
-// bits of e (its bits order as the values; NaN last), which resolve sizes to
-// under 1%, then the position. Keys are distinct, so the ranks within a
-// block are always a permutation.
-static_assert(kOrderMaxM <= 65536, "positions fill the low 16 bits of a key");
-__device__ __forceinline__ unsigned order_key(float e, int pos) {
-    const unsigned b = isnan(e) ? 0xffffffffu : __float_as_uint(e);
-    return (b & 0xffff0000u) | static_cast<unsigned>(pos);
+// Size class of a box size e >= 0: its quarter octave (the float's exponent
+// and top two mantissa bits; +inf and NaN land in the top class). Classes
+// order the queries of a block almost as well as exact sizes do (a CPU model
+// of the counts' scan: 0.261 against 0.256 of the frames visited) and let a
+// counting sort build the order in O(m).
+constexpr int kOrderClasses = 64;
+__device__ __forceinline__ unsigned size_bits(float e) {
+    return isnan(e) ? 0xffffffffu : __float_as_uint(fmaxf(e, 0.f)) >> 21;
 }
 
 // Writes out[rank] = pos in the block order for every storage position pos
-// of a grid of G x G cells (cell index `start`), with the keys in s_key[pos]
-// and cell_of(pos, row, col) giving each position's cell. Called by the
-// whole CTA after it has written s_key.
+// of a grid of G x G cells (cell index `start`), with the size bits of each
+// position in s_key[pos] (size_bits) and cell_of(pos, row, col) giving its
+// cell. The order is blocks in Z order, then classes ascending; within a
+// (block, class) bin the order is whatever the shared-memory atomics give
+// (any order gives the same results). Called by the whole CTA after it has
+// written s_key; overwrites s_key.
 template <class CellOf>
-__device__ void write_block_order(const unsigned* s_key, const int* start, int G, int m, CellOf cell_of,
+__device__ void write_block_order(unsigned* s_key, const int* start, int G, int m, CellOf cell_of,
                                   int* out) {
-    __shared__ int s_boff[kOrderBlocks * kOrderBlocks];
-    const int nb = (G + kOrderBlock - 1) / kOrderBlock;
-    // frames per block, then their exclusive prefix in Z order of the blocks
-    if (threadIdx.x < kOrderBlocks * kOrderBlocks) {
-        const int z = threadIdx.x;
-        int bx = 0, by = 0;
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            bx |= ((z >> (2 * b + 1)) & 1) << b;
-            by |= ((z >> (2 * b)) & 1) << b;
-        }
-        int n = 0;
-        if (bx < nb && by < nb) {
-            const int c0 = by * kOrderBlock, c1 = min(c0 + kOrderBlock, G);
-            for (int r = bx * kOrderBlock; r < min((bx + 1) * kOrderBlock, G); ++r) {
-                n += __ldg(start + r * G + c1) - __ldg(start + r * G + c0);
-            }
-        }
-        s_boff[z] = n;
-    }
+    constexpr int kBins = kOrderBlocks * kOrderBlocks * kOrderClasses;
+    __shared__ int s_bin[kBins];
+    __shared__ int s_part[kOrderThreads];
+    __shared__ unsigned s_lo;
+    for (int b = threadIdx.x; b < kBins; b += blockDim.x) s_bin[b] = 0;
+    if (threadIdx.x == 0) s_lo = 0xffffffffu;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        int acc = 0;
-        for (int z = 0; z < kOrderBlocks * kOrderBlocks; ++z) {
-            const int n = s_boff[z];
-            s_boff[z] = acc;
-            acc += n;
-        }
-    }
+    // the smallest class present becomes class 0
+    unsigned lo = 0xffffffffu;
+    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) lo = min(lo, s_key[pos]);
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    if ((threadIdx.x & 31) == 0) atomicMin(&s_lo, lo);
     __syncthreads();
+    lo = s_lo;
+    // bin of every position (block Z code, class), counted
     for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
         int row, col;
         cell_of(pos, row, col);
-        const int bx = row / kOrderBlock, by = col / kOrderBlock;
-        const unsigned key = s_key[pos];
-        const int c0 = by * kOrderBlock, c1 = min(c0 + kOrderBlock, G);
-        int rank = 0;
-        for (int r = bx * kOrderBlock; r < min((bx + 1) * kOrderBlock, G); ++r) {
-            const int lo = __ldg(start + r * G + c0), hi = __ldg(start + r * G + c1);
-            for (int q = lo; q < hi; ++q) rank += s_key[q] < key ? 1 : 0;
-        }
-        out[s_boff[block_zcode(bx, by)] + rank] = pos;
+        const unsigned d = s_key[pos] - lo;
+        const int cls = d < static_cast<unsigned>(kOrderClasses) ? static_cast<int>(d) : kOrderClasses - 1;
+        const int bin = block_zcode(row / kOrderBlock, col / kOrderBlock) * kOrderClasses + cls;
+        s_key[pos] = static_cast<unsigned>(bin);
+        atomicAdd(&s_bin[bin], 1);
     }
+    __syncthreads();
+    // exclusive prefix over the bins: kBins / kOrderThreads bins per thread
+    constexpr int kPer = kBins / kOrderThreads;
+    static_assert(kBins % kOrderThreads == 0, "bins split evenly over the CTA");
+    int acc = 0;
+    for (int q = 0; q < kPer; ++q) acc += s_bin[threadIdx.x * kPer + q];
+    s_part[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int t = 0; t < kOrderThreads; ++t) {
+            const int v = s_part[t];
+            s_part[t] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    int run = s_part[threadIdx.x];
+    for (int q = 0; q < kPer; ++q) {
+        const int b = threadIdx.x * kPer + q;
+        const int v = s_bin[b];
+        s_bin[b] = run;
+        run += v;
+    }
+    __syncthreads();
+    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) out[atomicAdd(&s_bin[s_key[pos]], 1)] = pos;
 }
 
 // Count order of one count group per CTA: key = the largest eps of the
@@ -421,7 +431,7 @@ __global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArg
         float e = __ldg(eps + o[0] + j);
 #pragma unroll
         for (int p = 1; p < kCountGroup; ++p) e = fmaxf(e, __ldg(eps + o[p] + j));
-        s_key[pos] = order_key(e, pos);
+        s_key[pos] = size_bits(e);
     }
     const auto cell_of = [&](int pos, int& row, int& col) {
         const int c = __ldg(nd.cell + __ldg(nd.perm + pos));
@@ -443,7 +453,7 @@ __global__ void __launch_bounds__(kOrderThreads) grid_pair_order_kernel(const Ks
     const int m = pairs[blockIdx.x].m, G = na.G;
     for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
         const int j = __ldg(gp.perm + pos);
-        s_key[pos] = order_key(fmaxf(__ldg(na.est + j), __ldg(nb.est + j)), pos);
+        s_key[pos] = size_bits(fmaxf(__ldg(na.est + j), __ldg(nb.est + j)));
     }
     const auto cell_of = [&](int pos, int& row, int& col) {
         const int j = __ldg(gp.perm + pos);

@@ -15,7 +15,10 @@
 // address; the first call on each device (with that device current) asks
 // the runtime for the array's device address with cudaGetSymbolAddress and
 // keeps it. That first call also copies the psi table into the area, so it
-// should be made before any stream capture. Every call uses the same area:
+// should be made before any stream capture. The address and the table are
+// kept until the process exits; a device reset by the host application
+// after the first call (cudaDeviceReset) is not supported, since it
+// discards both. Every call uses the same area:
 // calls whose work overlaps on the GPU (other streams, other threads) race
 // and must be serialised by the caller. Sizes above the limit are rejected.
 #include <cuda_runtime.h>

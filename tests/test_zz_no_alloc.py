@@ -48,7 +48,7 @@ def _reference_entry(Xd, m, k, d):
 
 
 @pytest.mark.parametrize("d,k,m", [(3, 6, 1000), (1, 4, 2000), (2, 10, 777)])
-def test_no_alloc_matches_allocating_entry_point_twice(d, k, m):
+def test_no_alloc_matches_allocating_entry_point_twice(oracle_mod, d, k, m):
     from netsci_gb300 import synthetic
     rng = np.random.default_rng(1000 + d * 10 + k)
     if d == 3:
@@ -64,6 +64,52 @@ def test_no_alloc_matches_allocating_entry_point_twice(d, k, m):
     second = _noalloc(Xd[0], Xd[1], ld, mm, k, d)
     # the kernels are shared with the allocating path: results are bit-exact
     assert first == want and second == want
+    # and MI equals the CPU oracle's (the reference CPU path's arithmetic)
+    assert first[0] == oracle_mod.mi_pair(X[0], X[1], m, k, d)
+
+
+def test_no_alloc_reproduces_the_reference_goldens(golden):
+    """The reference's own published MI values for its Gaussian fixtures
+    (tests/netcalc/python/test_MutualInformation.py:37,64), twice each."""
+    g = golden("gaussian")
+    for n in (1000, 2000):
+        Xd, m = _rows(np.stack([g[f"x{n}"], g[f"y{n}"]]), 1)
+        for _ in range(2):
+            mi, _ = _noalloc(Xd[0], Xd[1], Xd.shape[2], m, 4, 1)
+            assert mi == float(g[f"mi{n}"])
+    assert float(g["mi1000"]) == 0.8449974060058594
+    assert float(g["mi2000"]) == 0.8485465049743652
+
+
+def test_no_alloc_calls_allocate_no_device_memory():
+    """After the first call on the device, calls of different sizes leave the
+    device's free memory unchanged: nothing is allocated, by the library or
+    through it (inputs and outputs are made before the measurement)."""
+    from netsci_gb300 import synthetic
+    cases = []
+    for m, seed in ((300, 1), (4000, 2), (1500, 3), (9000, 4)):
+        X, _ = synthetic.protein_trajectory(2, m, seed=seed)
+        Xd, mm = _rows(X, 3)
+        cases.append((Xd, mm))
+    mi = torch.full((1,), float("nan"), device="cuda")
+    gc = torch.full((1,), float("nan"), device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def call(Xd, mm):
+        from netsci_gb300._lib import call as nsg_call
+        nsg_call("nsg_ksg_pair_noalloc_device", ctypes.c_void_p(Xd[0].data_ptr()),
+                 ctypes.c_void_p(Xd[1].data_ptr()), Xd.shape[2], mm, 6, 3,
+                 ctypes.c_void_p(mi.data_ptr()), ctypes.c_void_p(gc.data_ptr()),
+                 ctypes.c_void_p(stream.cuda_stream))
+    call(*cases[0])   # the first call on the device sets the area up
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for Xd, mm in cases * 2:
+        call(Xd, mm)
+        assert np.isfinite(float(mi.item())) and np.isfinite(float(gc.item()))
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
 
 
 def test_no_alloc_after_a_different_size_call():
