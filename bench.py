@@ -551,6 +551,7 @@ def main():
     barrier()
     dev_ms = ev0.elapsed_time(ev1)
     kms = [plans[s].kernel_ms() for s in range(args.warmup, S)]
+    tied = [plans[s].tied_samples() for s in range(args.warmup, S)]
     launches = sum(plans[s].launches for s in range(args.warmup, S))
     t_max = max_over_ranks(dev_ms) / 1000.0
     value = sharding.weak_scaling_value(world, args.steps, B, t_max)
@@ -595,6 +596,12 @@ def main():
                 "frac": count_ops / count_s / 1e9 / peak_gops,
                 "mix_ceiling_gops": ceil_count,
                 "frac_of_mix_ceiling": count_ops / count_s / 1e9 / ceil_count},
+            "ksg_tie_kernel": {
+                "ms_per_launch": statistics.mean(k[2] for k in kms),
+                "tied_samples_per_launch": statistics.mean(tied),
+                "note": ("samples whose k-th distance ties between frames with different "
+                         "marginals, replayed in the reference sort's order; O(m) per "
+                         "sample")},
         }
         dom = per_kernel["ksg_grid_pass1_kernel"]
         kernel, achieved, traffic = "ksg_grid_pass1_kernel", dom["achieved_gops"], None

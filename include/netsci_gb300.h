@@ -257,11 +257,16 @@ int nsg_ksg_plan_search(const nsg_ksg_plan* plan, int* mode);
  * pair; 0 for exhaustive plans. Synchronizes with the device. */
 int nsg_ksg_plan_evaluations(const nsg_ksg_plan* plan, unsigned long long* search,
                              unsigned long long* counts, unsigned long long* compares);
-/* Device milliseconds of the last run's search kernels and count kernels
- * (flag bit 1), summed over the plan's batches; the order kernels are not
- * included. An exhaustive plan's single kernel counts as search. Waits for
- * that run's events. */
-int nsg_ksg_plan_kernel_ms(const nsg_ksg_plan* plan, float* search_ms, float* count_ms);
+/* Device milliseconds of the last run's search kernels, count kernels and
+ * tie kernels (tie_ms nullable; flag bit 1), summed over the plan's batches;
+ * the order kernels are not included. An exhaustive plan's single kernel
+ * counts as search. Waits for that run's events. */
+int nsg_ksg_plan_kernel_ms(const nsg_ksg_plan* plan, float* search_ms, float* count_ms,
+                           float* tie_ms);
+/* Samples of the plan's last run whose k-th and (k+1)-th joint distances tie
+ * between frames with different marginals, i.e. that went to the tie kernel
+ * to replay the reference sort's order. Synchronizes with the device. */
+int nsg_ksg_plan_tied_samples(const nsg_ksg_plan* plan, long long* n);
 
 /* One pair's MI / GC without any device allocation. No counterpart in the
  * reference: it is for callers that cannot allocate device memory, such as

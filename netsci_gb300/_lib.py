@@ -138,7 +138,9 @@ _SIGNATURES = {
     "nsg_measure_issue_ceiling": (c_int, [c_int, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double)]),
     "nsg_ksg_plan_search": (c_int, [c_void_p, P_int]),
+    "nsg_ksg_plan_tied_samples": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "nsg_ksg_plan_kernel_ms": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float),
+                                       ctypes.POINTER(ctypes.c_float),
                                        ctypes.POINTER(ctypes.c_float)]),
     "nsg_ksg_plan_evaluations": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_ulonglong),
                                          ctypes.POINTER(ctypes.c_ulonglong),

@@ -514,11 +514,20 @@ int nsg_ksg_plan_evaluations(const nsg_ksg_plan* plan, unsigned long long* searc
     });
 }
 
-int nsg_ksg_plan_kernel_ms(const nsg_ksg_plan* plan, float* search_ms, float* count_ms) {
+int nsg_ksg_plan_tied_samples(const nsg_ksg_plan* plan, long long* n) {
+    return guarded([&] {
+        if (!plan || !plan->plan) nsg::invalid("plan is null");
+        if (!n) nsg::invalid("null output");
+        *n = plan->plan->tied_samples();
+    });
+}
+
+int nsg_ksg_plan_kernel_ms(const nsg_ksg_plan* plan, float* search_ms, float* count_ms,
+                           float* tie_ms) {
     return guarded([&] {
         if (!plan || !plan->plan) nsg::invalid("plan is null");
         if (!search_ms || !count_ms) nsg::invalid("null output");
-        plan->plan->kernel_ms(search_ms, count_ms);
+        plan->plan->kernel_ms(search_ms, count_ms, tie_ms);
     });
 }
 

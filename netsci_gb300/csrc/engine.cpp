@@ -268,8 +268,8 @@ long long count_items(const std::vector<nsg_ksg_pair>& pairs, int qc) {
 }  // namespace
 
 // Timing events per batch: search begin, search end, counts begin (after
-// the count-order kernel), counts end.
-constexpr int kEventsPerBatch = 4;
+// the count-order kernel), counts end, tie kernel begin, tie kernel end.
+constexpr int kEventsPerBatch = 6;
 
 KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const KsgOutputs& out,
                  const KsgPlanOptions& opt)
@@ -581,7 +581,7 @@ void KsgPlan::enqueue(cudaStream_t s) {
         entry_->launch(a, b.grid, s);
         NSG_CUDA(cudaGetLastError());
         if (timing_) {
-            for (int j = 1; j < kEventsPerBatch; ++j) record_event(ev[j], s);
+            for (int j = 1; j < 5; ++j) record_event(ev[j], s);
         }
         KsgTieArgs t{};
         t.pairs = pairs_dev_.as<KsgPairDesc>();
@@ -601,6 +601,7 @@ void KsgPlan::enqueue(cudaStream_t s) {
         t.idx = tie_idx_.as<int>();
         t.stride = tie_stride_;
         ksg_launch_ties(t, d_, s);
+        if (timing_) record_event(ev[5], s);
         KsgFinalArgs f{};
         f.pairs = pairs_dev_.as<KsgPairDesc>() + b.pair0;
         f.npairs = b.npairs;
@@ -819,7 +820,9 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         t.dz = tie_dz_.as<float>();
         t.idx = tie_idx_.as<int>();
         t.stride = tie_stride_;
+        if (timing_) record_event(ev[4], s);
         ksg_launch_ties(t, d_, s);
+        if (timing_) record_event(ev[5], s);
         KsgFinalArgs f{};
         f.pairs = bp;
         f.npairs = b.npairs;
@@ -851,6 +854,16 @@ int KsgPlan::launches() const {
 }
 
 int KsgPlan::staging() const { return entry_ ? entry_->tma : 0; }
+
+long long KsgPlan::tied_samples() const {
+    if (batches_.empty()) return 0;
+    std::vector<int> h(kCounters * batches_.size());
+    NSG_CUDA(cudaMemcpy(h.data(), counters_.get(), h.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    long long n = 0;
+    const int slot = search_ ? 2 : 1;  // the tie-list count of each batch
+    for (size_t b = 0; b < batches_.size(); ++b) n += h[kCounters * b + slot];
+    return n;
+}
 
 void KsgPlan::evaluations(unsigned long long* search, unsigned long long* counts,
                           unsigned long long* compares) const {
@@ -968,24 +981,27 @@ KsgTuned ksg_autotune(const std::vector<nsg_ksg_pair>& pairs, int k, int d) {
 
 float KsgPlan::count_ms() const {
     float search = 0.f, counts = 0.f;
-    kernel_ms(&search, &counts);
+    kernel_ms(&search, &counts, nullptr);
     return search + counts;
 }
 
-void KsgPlan::kernel_ms(float* search_ms, float* count_ms) const {
+void KsgPlan::kernel_ms(float* search_ms, float* count_ms, float* tie_ms) const {
     if (!timing_) fail(NSG_ERR_INVALID, "plan was created without timing events");
-    float search = 0.f, counts = 0.f;
+    float search = 0.f, counts = 0.f, ties = 0.f;
     for (size_t b = 0; b < batches_.size(); ++b) {
         const cudaEvent_t* ev = events_.data() + kEventsPerBatch * b;
-        NSG_CUDA(cudaEventSynchronize(ev[3]));
+        NSG_CUDA(cudaEventSynchronize(ev[5]));
         float ms = 0.f;
         NSG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
         search += ms;
         NSG_CUDA(cudaEventElapsedTime(&ms, ev[2], ev[3]));
         counts += ms;
+        NSG_CUDA(cudaEventElapsedTime(&ms, ev[4], ev[5]));
+        ties += ms;
     }
     *search_ms = search;
     *count_ms = counts;
+    if (tie_ms) *tie_ms = ties;
 }
 
 void KsgPlan::run(cudaStream_t s) {

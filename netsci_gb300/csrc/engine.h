@@ -95,9 +95,12 @@ public:
     // Synchronizes with the device.
     void evaluations(unsigned long long* search, unsigned long long* counts,
                      unsigned long long* compares = nullptr) const;
+    // Samples the last run sent to the tie kernel (the reference sort's order
+    // replayed); synchronizes with the device.
+    long long tied_samples() const;
     // Device milliseconds of the last run's search kernels and count kernels
     // (the order kernels excluded), summed over batches; needs timing.
-    void kernel_ms(float* search_ms, float* count_ms) const;
+    void kernel_ms(float* search_ms, float* count_ms, float* tie_ms = nullptr) const;
 
 private:
     struct Batch {

@@ -62,10 +62,11 @@ __device__ __forceinline__ float tie_marginal(const float (&q)[D], const float* 
 // the latter; the elements between them are untouched until then, so the
 // stoppers can be read from the array as it was. The cut is the first left
 // stopper past the last swap, or that swap's right position if it comes
-// first. Lane 0 holds the segment stack and does the swaps; all lanes load
-// and vote. A segment whose depth budget runs out is heapsorted by lane 0
-// (heap_sort_like_reference). Same result as the serial routine, element for
-// element.
+// first. The pairs found by one round of ballots touch distinct positions,
+// so lane t swaps the round's t-th pair, all at once. Lane 0 holds the
+// segment stack; all lanes load and vote. A segment whose depth budget runs
+// out is heapsorted by lane 0 (heap_sort_like_reference). Same result as the
+// serial routine, element for element.
 __device__ bool sort_prefix_warp(const float* key, int* idx, int n, int T, SortSegment* stack,
                                  int cap, int lane) {
     if (n <= 1) return true;
@@ -143,20 +144,34 @@ __device__ bool sort_prefix_warp(const float* key, int* idx, int n, int T, SortS
                 // the median of three leaves stoppers on both sides; running
                 // out of either means a broken invariant, reported as failure
                 if (rend) return false;
-                const int lpos = lend ? 0x7fffffff : lchunk + __ffs(lmask) - 1;
-                const int rpos = rchunk - (__ffs(rmask) - 1);
-                if (lpos < rpos) {
-                    if (lane == 0) {
-                        const int t = idx[lpos];
-                        idx[lpos] = idx[rpos];
-                        idx[rpos] = t;
+                // the t-th left stopper of lmask pairs with the t-th right
+                // stopper of rmask while it lies left of it; those pairs form
+                // a prefix of t and are swapped together, lane t taking pair t
+                const int npair = lend ? 0 : min(__popc(lmask), __popc(rmask));
+                int lp = 0x7fffffff, rp = -1;
+                if (lane < npair) {
+                    lp = lchunk + static_cast<int>(__fns(lmask, 0, lane + 1));
+                    rp = rchunk - static_cast<int>(__fns(rmask, 0, lane + 1));
+                }
+                const bool swap = lane < npair && lp < rp;
+                const int c = __popc(__ballot_sync(kFull, swap));
+                if (swap) {
+                    const int t = idx[lp];
+                    idx[lp] = idx[rp];
+                    idx[rp] = t;
+                }
+                __syncwarp();
+                if (c > 0) prev_r = __shfl_sync(kFull, rp, c - 1);
+                if (c == npair && !lend) {
+                    // every pair of the round swapped: drop them, continue
+                    for (int q = 0; q < c; ++q) {
+                        lmask &= lmask - 1;
+                        rmask &= rmask - 1;
                     }
-                    __syncwarp();
-                    lmask &= lmask - 1;
-                    rmask &= rmask - 1;
-                    prev_r = rpos;
                     continue;
                 }
+                // pair c crosses (or no left stopper is left)
+                const int lpos = lend ? 0x7fffffff : __shfl_sync(kFull, lp, c);
                 cut = prev_r < 0 ? lpos : min(lpos, prev_r);
                 break;
             }

@@ -631,8 +631,11 @@ void Server::ksg_loop() {
                 }
             }
             if (active.empty()) continue;
-            // fair share of the tick's work, then the rest in arrival order
-            const double share = cfg_.tick_ops / active.size();
+            // Short jobs first: a job whose remaining work fits in a quarter
+            // of the tick takes all of it, so short requests never wait behind
+            // long ones. The rest of the tick goes to jobs in arrival order, so
+            // the oldest long job advances at nearly the whole GPU's rate (as
+            // if served alone) instead of sharing it with every later one.
             double used_ops = 0;
             long long used_pairs = 0, used_samples = 0;
             std::vector<long long> take(active.size(), 0);
@@ -644,12 +647,17 @@ void Server::ksg_loop() {
                     // a pair's work; pairs searched on cell grids evaluate about 40% of it
                     const double per = 8.0 * j.d * j.n * (j.n - 1.0) *
                                        (j.slots.size() == j.pairs.size() && j.n >= kGridMinSamples ? 0.4 : 1.0);
-                    const double budget = pass == 0 ? share : cfg_.tick_ops - used_ops;
-                    long long t = std::max<long long>(1, static_cast<long long>(budget / per));
+                    long long t;
+                    if (pass == 0) {
+                        if (remaining * per > cfg_.tick_ops / 4 || used_ops + remaining * per > cfg_.tick_ops) continue;
+                        t = remaining;
+                    } else {
+                        if (used_ops >= cfg_.tick_ops) break;
+                        t = std::max<long long>(1, static_cast<long long>((cfg_.tick_ops - used_ops) / per));
+                    }
                     t = std::min(t, remaining);
                     t = std::min(t, cap_pairs_ - used_pairs);
                     t = std::min(t, (cap_samples_ - used_samples) / std::max(1, j.n));
-                    if (pass == 1 && used_ops >= cfg_.tick_ops) t = 0;
                     if (t <= 0) continue;
                     take[i] += t;
                     used_ops += t * per;

@@ -3,11 +3,12 @@
 // Jobs arrive through submit_*() from any thread. A scheduler thread admits
 // them in arrival order whenever their device footprint fits the memory
 // budget (a later, smaller job may be admitted while an earlier, larger one
-// waits), and runs "ticks": each tick takes pairs from every admitted KSG job
-// (an equal share of the tick's work for each job first, then the rest in
-// arrival order), puts them in one work queue and runs the count, tie and
-// finalize kernels once over it. Jobs that arrive while a tick runs join the
-// next one. APSP jobs run on their own stream and worker thread, so their
+// waits), and runs "ticks": each tick takes pairs from the admitted KSG jobs
+// (first every job whose remaining work fits in a quarter of the tick, whole;
+// then the rest of the tick in arrival order, so the oldest long job runs at
+// nearly the full rate), puts them in one work queue and runs the count, tie
+// and finalize kernels once over it. Jobs that arrive while a tick runs join
+// the next one. APSP jobs run on their own stream and worker thread, so their
 // kernels overlap the KSG ticks on the device. Trajectories can be
 // registered once and stay resident in HBM for any number of jobs.
 #pragma once

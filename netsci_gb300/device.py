@@ -143,12 +143,18 @@ class KsgPlan:
              ctypes.byref(c))
         return a.value, b.value, c.value
 
-    def kernel_ms(self) -> tuple[float, float]:
-        """Device ms of the last run's (search, count) kernels, order kernels
-        excluded; plans need timing=True."""
-        a, b = ctypes.c_float(), ctypes.c_float()
-        call("nsg_ksg_plan_kernel_ms", self._h, ctypes.byref(a), ctypes.byref(b))
-        return float(a.value), float(b.value)
+    def tied_samples(self) -> int:
+        """Samples of the last run that went to the tie kernel."""
+        v = ctypes.c_longlong()
+        call("nsg_ksg_plan_tied_samples", self._h, ctypes.byref(v))
+        return v.value
+
+    def kernel_ms(self) -> tuple[float, float, float]:
+        """Device ms of the last run's (search, count, tie) kernels, order
+        kernels excluded; plans need timing=True."""
+        a, b, c = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+        call("nsg_ksg_plan_kernel_ms", self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return float(a.value), float(b.value), float(c.value)
 
     def count_ms(self) -> float:
         """Device time (ms) of the count kernels in the last run."""
