@@ -127,6 +127,24 @@ def test_large_m_pair_per_sample(oracle_mod, knobs, m, seed):
         _same(_detail(X[0], X[2], m, 6, 3), det, mi)
 
 
+def test_block_orders_at_their_largest_m_on_a_correlated_pair(oracle_mod, knobs):
+    """m = 40960, the largest m the block orders take, on a pair whose two
+    rows are nearly the same motion: its frames crowd the diagonal blocks of
+    the pair grid, the case that made ranking a query against its whole
+    block quadratic. The orders are built by counting sort now; every
+    per-sample output still equals the oracle's."""
+    from netsci_gb300 import synthetic
+    m = 40960
+    X, _ = synthetic.protein_trajectory(2, m, seed=4096)
+    rng = np.random.default_rng(4096)
+    xa = X[0]
+    xb = (xa + 0.05 * rng.standard_normal(xa.size)).astype(np.float32)
+    mi, det = oracle_mod.mi_pair(xa, xb, m, 6, 3, detail=True, threads=THREADS)
+    knobs.set_ksg_search(1)
+    knobs.set_ksg_orders(1)
+    _same(_detail(xa, xb, m, 6, 3), det, mi)
+
+
 def test_gaussian_mi_largest_request(oracle_mod, knobs):
     """The serving mix's Gaussian MI at n = 20000, d = 1, k = 4, on both
     searches and through the reference's per-pair call."""
