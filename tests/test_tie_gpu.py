@@ -5,7 +5,8 @@ reference CPU path's std::sort order, netcalc/src/mutual_information_cpu.cpp:
 * tie-saturated pairs: coordinates on a coarse grid, where nearly every
   sample ties at the k-th distance between frames with different marginals,
   so nearly every sample goes to the tie list (the list holds every sample of
-  a batch and cannot overflow);
+  a batch and cannot overflow), for k up to 62 (the replayed eps then spans
+  more sorted positions than a warp has lanes);
 * a sample whose distance row defeats the median-of-three pivots, so that
   the reference's introsort runs out of depth budget and heapsorts the
   segment holding the neighbours, with a tie at the k-th distance (keys made
@@ -62,7 +63,8 @@ def _same(out, det, mi):
 
 
 @pytest.mark.parametrize("d,k,n,levels", [(1, 4, 6000, 64), (2, 6, 5000, 32), (3, 6, 4000, 32),
-                                          (3, 10, 2500, 32)])
+                                          (3, 10, 2500, 32), (2, 40, 3000, 32), (1, 45, 4000, 64),
+                                          (3, 62, 2600, 16)])
 def test_tie_saturated_pair(oracle_mod, search, d, k, n, levels):
     rng = np.random.default_rng(n + levels)
     xa = rng.integers(0, levels, d * n).astype(np.float32)
