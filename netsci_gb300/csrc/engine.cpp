@@ -527,11 +527,8 @@ KsgPlan::KsgPlan(const std::vector<nsg_ksg_pair>& pairs_in, int k, int d, const 
         tie_cap_ = static_cast<int>(std::min<long long>(std::max<long long>(1, batch_samples), 1LL << 30));
         ties_.reset(static_cast<size_t>(tie_cap_) * sizeof(KsgTie));
         tie_stride_ = maxm;
-        // rows of m up to ksg_tie_smem_max_m() live in the tie kernel's
-        // shared memory; larger ones need a global row per tie warp
-        const bool rows_global = tie_stride_ > ksg_tie_smem_max_m();
-        tie_dz_.reset(rows_global ? static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(float) : 16);
-        tie_idx_.reset(rows_global ? static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(int) : 16);
+        tie_dz_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(float));
+        tie_idx_.reset(static_cast<size_t>(ksg_tie_warps()) * tie_stride_ * sizeof(int));
         fault_.reset(sizeof(int));
         NSG_CUDA(cudaMemset(fault_.get(), 0, sizeof(int)));
         psi_ = device_psi(maxm);

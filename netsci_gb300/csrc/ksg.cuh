@@ -105,9 +105,6 @@ void ksg_launch_counts(const KsgCountArgs& a, int d, int kmax, const KsgShape& s
 void ksg_launch_final(const KsgFinalArgs& a, cudaStream_t st);
 // Warps the tie kernel runs with (scratch rows needed).
 int ksg_tie_warps();
-// Largest m whose tie rows ksg_launch_ties keeps in shared memory (one CTA
-// per tied sample); plans with a larger m need ksg_tie_warps() global rows.
-int ksg_tie_smem_max_m();
 void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st);
 void ksg_launch_ties_ctas(const KsgTieArgs& a, int d, int ctas, cudaStream_t st);
 // One pair with all scratch in the library's static device area

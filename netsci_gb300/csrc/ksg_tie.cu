@@ -284,158 +284,11 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, kCtasPerSm) ksg_tie_kernel(
     }
 }
 
-// One CTA per tied sample, its distance row and index array in shared
-// memory (pairs with m <= kTieSmemMaxM). The O(m) steps -- the distance row
-// and the recount -- run on all 256 threads; warp 0 replays the sort on the
-// shared arrays, where each ballot round's loads take tens of cycles instead
-// of a global-memory round trip. Same arithmetic and same replay as
-// ksg_tie_kernel.
-constexpr int kTieBlockThreads = 256;
-constexpr int kTieBlockWarps = kTieBlockThreads / 32;
-constexpr int kTieSmemMaxM = 20480;  // 8 bytes per frame: 160 KB
-
-template <int D>
-__global__ void __launch_bounds__(kTieBlockThreads) ksg_tie_block_kernel(KsgTieArgs A, int cap_m) {
-    extern __shared__ __align__(16) unsigned char s_raw[];
-    float* dz = reinterpret_cast<float*>(s_raw);
-    int* idx = reinterpret_cast<int*>(s_raw + sizeof(float) * static_cast<size_t>(cap_m));
-    __shared__ SortSegment s_stack[kStack];
-    __shared__ int s_e, s_ok;
-    __shared__ float s_ea[kTieBlockWarps], s_eb[kTieBlockWarps];
-    __shared__ int s_ca[kTieBlockWarps], s_cb[kTieBlockWarps];
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int total = min(*A.tie_count, A.tie_cap);
-    for (;;) {
-        __syncthreads();  // the previous sample's shared values are read
-        if (tid == 0) s_e = atomicAdd(A.tie_next, 1);
-        __syncthreads();
-        const int e = s_e;
-        if (e >= total) return;
-        const KsgTie t = A.ties[e];
-        const KsgPairDesc P = A.pairs[t.pair];
-        const int m = P.m, ld = P.ld;
-        const int* __restrict__ fmap = P.fmap;
-        const float* __restrict__ xa = P.xa;
-        const float* __restrict__ xb = P.xb;
-        if (m > cap_m) {  // the launcher sizes the rows for every pair
-            if (tid == 0) atomicOr(A.fault, FAULT_BAD_INDEX);
-            continue;
-        }
-        const int sq = tie_frame(fmap, t.q, ld, A.fault);
-        float qa[D], qb[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) {
-            qa[c] = __ldg(xa + (size_t)c * ld + sq);
-            qb[c] = __ldg(xb + (size_t)c * ld + sq);
-        }
-        for (int j = tid; j < m; j += kTieBlockThreads) {
-            const int s = tie_frame(fmap, j, ld, A.fault);
-            dz[j] = fmaxf(tie_marginal<D>(qa, xa, ld, s), tie_marginal<D>(qb, xb, ld, s));
-            idx[j] = j;
-        }
-        __syncthreads();
-        if (wid == 0) {
-            const bool ok = sort_prefix_warp(dz, idx, m, A.k + 1, s_stack, kStack, lane);
-            if (lane == 0) s_ok = ok ? 1 : 0;
-        }
-        __syncthreads();
-        if (!s_ok) {
-            if (tid == 0) atomicOr(A.fault, FAULT_TIE_UNRESOLVED);
-            continue;
-        }
-        // eps over sorted positions 1..k
-        float ea = 0.f, eb = 0.f;
-        for (int p = 1 + tid; p <= A.k; p += kTieBlockThreads) {
-            const int s = tie_frame(fmap, idx[p], ld, A.fault);
-            ea = fmaxf(ea, tie_marginal<D>(qa, xa, ld, s));
-            eb = fmaxf(eb, tie_marginal<D>(qb, xb, ld, s));
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            ea = fmaxf(ea, __shfl_xor_sync(kFull, ea, off));
-            eb = fmaxf(eb, __shfl_xor_sync(kFull, eb, off));
-        }
-        if (lane == 0) {
-            s_ea[wid] = ea;
-            s_eb[wid] = eb;
-        }
-        __syncthreads();
-        ea = s_ea[0];
-        eb = s_eb[0];
-#pragma unroll
-        for (int w = 1; w < kTieBlockWarps; ++w) {
-            ea = fmaxf(ea, s_ea[w]);
-            eb = fmaxf(eb, s_eb[w]);
-        }
-        // marginal counts over all frames
-        int ca = 0, cb = 0;
-        for (int j0 = wid * 32; j0 < m; j0 += kTieBlockThreads) {
-            const int j = j0 + lane;
-            bool pa = false, pb = false;
-            if (j < m) {
-                const int s = tie_frame(fmap, j, ld, A.fault);
-                pa = tie_marginal<D>(qa, xa, ld, s) <= ea;
-                pb = tie_marginal<D>(qb, xb, ld, s) <= eb;
-            }
-            ca += __popc(__ballot_sync(kFull, pa));
-            cb += __popc(__ballot_sync(kFull, pb));
-        }
-        if (lane == 0) {
-            s_ca[wid] = ca;
-            s_cb[wid] = cb;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            ca = 0;
-            cb = 0;
-#pragma unroll
-            for (int w = 0; w < kTieBlockWarps; ++w) {
-                ca += s_ca[w];
-                cb += s_cb[w];
-            }
-            const long long o = P.scratch + t.q;
-            const int nx = min(max(ca - 1, 0), m);
-            const int ny = min(max(cb - 1, 0), m);
-            A.psum[o] = __fadd_rn(__ldg(A.psi + nx), __ldg(A.psi + ny));
-            if (A.nx) A.nx[o] = nx;
-            if (A.ny) A.ny[o] = ny;
-            if (A.eps_x) A.eps_x[o] = ea;
-            if (A.eps_y) A.eps_y[o] = eb;
-        }
-    }
-}
-
-template <int D>
-void launch_tie_block(const KsgTieArgs& a, int cap_m, cudaStream_t st) {
-    const size_t smem = 8 * static_cast<size_t>(cap_m);
-    // set on every launch: the attribute belongs to the current device
-    NSG_CUDA(cudaFuncSetAttribute(ksg_tie_block_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(8 * static_cast<size_t>(kTieSmemMaxM))));
-    int per_sm = 0;
-    NSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksg_tie_block_kernel<D>, kTieBlockThreads,
-                                                           smem));
-    ksg_tie_block_kernel<D><<<sm_count() * (per_sm > 0 ? per_sm : 1), kTieBlockThreads, smem, st>>>(a, cap_m);
-}
-
 }  // namespace
-
-int ksg_tie_smem_max_m() { return kTieSmemMaxM; }
 
 int ksg_tie_warps() { return sm_count() * kCtasPerSm * kWarpsPerCta; }
 
 void ksg_launch_ties(const KsgTieArgs& a, int d, cudaStream_t st) {
-    if (a.stride <= kTieSmemMaxM) {
-        // rows in shared memory: a.stride (the plan's largest m) sizes them
-        const int cap_m = static_cast<int>(a.stride);
-        switch (d) {
-            case 1: launch_tie_block<1>(a, cap_m, st); break;
-            case 2: launch_tie_block<2>(a, cap_m, st); break;
-            case 3: launch_tie_block<3>(a, cap_m, st); break;
-            default: fail(NSG_ERR_INVALID, "d must be 1, 2 or 3");
-        }
-        NSG_CUDA(cudaGetLastError());
-        return;
-    }
     const int grid = sm_count() * kCtasPerSm;
     const int threads = kWarpsPerCta * 32;
     switch (d) {
