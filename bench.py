@@ -80,9 +80,9 @@ sys.path.insert(0, str(ROOT / "netsci_gb300" / "dropin"))
 N_NODES, M_FRAMES, DIM, K_NN = 2000, 10000, 3, 6
 # DRAM bytes per pair of the search kernel at m = 10000, from an ncu capture
 # of a 256-pair step of this workload (profiles/ksg_grid_kernels_N2000_m10000.md:
-# 112.1 MB read + 15.0 MB written); the traffic is per pair (each pair's grid
+# 120.3 MB read + 15.8 MB written); the traffic is per pair (each pair's grid
 # copies), so it scales with the pairs.
-SEARCH_DRAM_BYTES_PER_PAIR = (112.1 + 15.0) * 1e6 / 256
+SEARCH_DRAM_BYTES_PER_PAIR = (120.3 + 15.8) * 1e6 / 256
 SEED = 2000
 METRIC = "GC pairs/sec (batched persistent), N=2000 nodes, m=10000 frames"
 
