@@ -326,8 +326,10 @@ int nsg_row_stats_device(const float* a, float* u, float* sigma, int m, int n, v
  * input and output buffers that must stay valid until the job is done. A
  * scheduler thread admits jobs when their device footprint fits
  * budget_bytes and runs ticks of about tick_ops algorithmic operations, each
- * one persistent launch over pairs of every admitted MI/GC job; jobs that
- * arrive meanwhile join the next tick. APSP jobs run on their own stream.
+ * one persistent launch over pairs of the admitted MI/GC jobs: first every
+ * job whose remaining work fits in a quarter of a tick, whole, then the rest
+ * of the tick in arrival order; jobs that arrive meanwhile join the next
+ * tick. APSP jobs run on their own stream.
  * Registered trajectories stay resident in HBM. Job states: 0 pending,
  * 1 running, 2 done, 3 failed. Times are seconds on the host steady clock. */
 typedef struct nsg_server nsg_server;
