@@ -26,7 +26,7 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["ksg_d1.cu", "ksg_d2.cu", "ksg_d3.cu", "ksg.cu", "ksg_tie.cu", "ksg_noalloc.cu", "apsp.cu",
-              "rowstats.cu", "node_com.cu", "ksg_grid.cu", "ceiling.cu"]
+              "rowstats.cu", "node_com.cu", "ksg_grid.cu", "ksg_grid_rec.cu", "ceiling.cu"]
 CPP_SOURCES = ["cuarray.cpp", "npy.cpp", "engine.cpp", "ksg_cpu.cpp", "netcalc.cpp", "serve.cpp", "capi.cpp",
                "dcd.cpp", "netchem.cpp"]
 

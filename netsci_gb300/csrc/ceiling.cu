@@ -56,7 +56,8 @@ __global__ void __launch_bounds__(32 * kGridWarps, 4)
     bool self_seen = false, tied = false;
     for (int r = 0; r < reps; ++r) {
         const int h = (r & 1) * kMixFrames;
-        gridk::pass1_chunk<D, KL>(tile + h, jt + h, kMixFrames, qa, qb, bd, bj, self_seen, tied);
+        gridk::pass1_chunk<D, KL, false>(tile + h, jt + h, kMixFrames, qa, qb, bd, bj, self_seen, tied, nullptr,
+                                         nullptr);
     }
     if (self_seen || tied || bj[0] != -1) atomicAdd(sink, 1ull);
 }

@@ -794,7 +794,7 @@ void KsgPlan::enqueue_grid(cudaStream_t s) {
         a.corder_ld = g.batch_maxm[bi];
         cudaEvent_t* ev = events_.data() + kEventsPerBatch * bi;
         if (timing_) record_event(ev[0], s);
-        grid_launch_search(a, d_, kmax_, g.search_grid, s);
+        grid_launch_search(a, d_, kmax_, g.search_grid, bootstrap_, s);
         if (timing_) record_event(ev[1], s);
         a.counter = ctr + 1;
         const GridArgs c = grid_launch_count_order(a, s);

@@ -327,70 +327,62 @@ __global__ void grid_combine_kernel(const KsgPairDesc* pairs, const int* cnt_a, 
     }
 }
 
-// Block orders of queries (see kOrderBlock). A warp's queries then sit in
-// one block of cells with boxes of similar size, so the union of their boxes
-// is smaller than in a grid's Z order of cells (by about a sixth for the
-// counts at m = 10000). Any order gives the same results; these only shorten
-// the scans.
+// Query orders (see kOrderBits and kOrderBlock). A warp's queries then have
+// boxes of nearly the same cells, so the union of their boxes is smaller
+// than in a grid's Z order of cells. Any order gives the same results;
+// these only shorten the scans.
 constexpr int kOrderThreads = 256;
-constexpr int kOrderBlocks = (kGridMaxG + kOrderBlock - 1) / kOrderBlock;  // per axis
-static_assert(kOrderBlocks <= 8, "block Z codes use three bits per axis");
+constexpr int kOrderKeyBits = 4 * kOrderBits;          // Z code of the four box corners
+constexpr int kOrderBins = 1 << (kOrderKeyBits - 4);   // counting-sort bins: the top bits
+constexpr int kOrderSortMax = 32;
+// Counts orders sort their bins on the low key bits up to this m (keys and
+// bins: 8 bytes per query of shared memory).
+constexpr int kOrderSortLowMaxM = 20480;
+static_assert(2 * kOrderSortLowMaxM <= kOrderMaxM, "the attribute covers both arrays");
+static_assert(kOrderBins % kOrderThreads == 0, "bins split evenly over the CTA");
 
-__device__ __forceinline__ int block_zcode(int bx, int by) {
-    int z = 0;
-#pragma unroll
-    for (int b = 0; b < 3; ++b) z |= ((bx >> b) & 1) << (2 * b + 1) | ((by >> b) & 1) << (2 * b);
-    return z;
+// Coarse cell (cell >> 1: kOrderBits bits) of x on an axis whose edges give
+// the thresholds t[L - 1] = e[2L - 1], L = 1..15, padded with +inf where the
+// grid has fewer cells and ended by a NaN (never <= x): the number of
+// thresholds <= x, by four branch-free steps over the 16 sorted entries.
+static_assert(kOrderBits == 4 && kGridMaxG <= 32, "coarse cells are cell pairs of a grid of <= 32 cells");
+__device__ __forceinline__ unsigned coarse_cell(const float* t, float x) {
+    unsigned b = t[7] <= x ? 8u : 0u;
+    b += t[b + 3] <= x ? 4u : 0u;
+    b += t[b + 1] <= x ? 2u : 0u;
+    b += t[b] <= x ? 1u : 0u;
+    return b;
 }
 
-// Size class of a box size e >= 0: its quarter octave (the float's exponent
-// and top two mantissa bits; +inf and NaN land in the top class). Classes
-// order the queries of a block almost as well as exact sizes do (a CPU model
-// of the counts' scan: 0.261 against 0.256 of the frames visited) and let a
-// counting sort build the order in O(m).
-constexpr int kOrderClasses = 64;
-__device__ __forceinline__ unsigned size_bits(float e) {
-    return isnan(e) ? 0xffffffffu : __float_as_uint(fmaxf(e, 0.f)) >> 21;
+// Bits of v < 16 spread to positions 0, 4, 8, 12.
+__device__ __forceinline__ unsigned spread4(unsigned v) {
+    return (v & 1u) | (v & 2u) << 3 | (v & 4u) << 6 | (v & 8u) << 9;
 }
 
-// Writes out[rank] = pos in the block order for every storage position pos
-// of a grid of G x G cells (cell index `start`), with the size bits of each
-// position in s_key[pos] (size_bits) and cell_of(pos, row, col) giving its
-// cell. The order is blocks in Z order, then classes ascending; within a
-// (block, class) bin the order is whatever the shared-memory atomics give
-// (any order gives the same results). Called by the whole CTA after it has
-// written s_key; overwrites s_key.
-template <class CellOf>
-__device__ void write_block_order(unsigned* s_key, const int* start, int G, int m, CellOf cell_of,
-                                  int* out) {
-    constexpr int kBins = kOrderBlocks * kOrderBlocks * kOrderClasses;
-    __shared__ int s_bin[kBins];
+// Z code of the box [x - h, x + h] x [y - h, y + h] in coarse cells: bit b
+// of corner q (low row, low column, high row, high column) at bit 4b + q.
+__device__ __forceinline__ unsigned box_key(const float* t1, const float* t2, float x, float y, float h) {
+    return spread4(coarse_cell(t1, x - h)) | spread4(coarse_cell(t2, y - h)) << 1 |
+           spread4(coarse_cell(t1, x + h)) << 2 | spread4(coarse_cell(t2, y + h)) << 3;
+}
+
+// Writes out[rank] = pos for every position pos < m of a grid, ranks in
+// ascending order of the 16-bit keys s_key[pos]: a counting sort on the top
+// twelve bits (shared-memory atomics). With s_tmp (m more words of shared
+// memory; m <= 65536) each bin of at most kOrderSortMax positions, most
+// bins, is then sorted on the low four bits by one thread in shared memory;
+// larger bins, where many queries share one box, keep the atomics' order,
+// so the work stays O(m). Without s_tmp the low bits are ignored. Called by
+// the whole CTA after it has written s_key.
+__device__ void write_key_order(const unsigned* s_key, int m, int* out, unsigned* s_tmp) {
+    __shared__ int s_bin[kOrderBins];
     __shared__ int s_part[kOrderThreads];
-    __shared__ unsigned s_lo;
-    for (int b = threadIdx.x; b < kBins; b += blockDim.x) s_bin[b] = 0;
-    if (threadIdx.x == 0) s_lo = 0xffffffffu;
+    for (int b = threadIdx.x; b < kOrderBins; b += blockDim.x) s_bin[b] = 0;
     __syncthreads();
-    // the smallest class present becomes class 0
-    unsigned lo = 0xffffffffu;
-    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) lo = min(lo, s_key[pos]);
-    lo = __reduce_min_sync(0xffffffffu, lo);
-    if ((threadIdx.x & 31) == 0) atomicMin(&s_lo, lo);
+    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) atomicAdd(&s_bin[s_key[pos] >> 4], 1);
     __syncthreads();
-    lo = s_lo;
-    // bin of every position (block Z code, class), counted
-    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
-        int row, col;
-        cell_of(pos, row, col);
-        const unsigned d = s_key[pos] - lo;
-        const int cls = d < static_cast<unsigned>(kOrderClasses) ? static_cast<int>(d) : kOrderClasses - 1;
-        const int bin = block_zcode(row / kOrderBlock, col / kOrderBlock) * kOrderClasses + cls;
-        s_key[pos] = static_cast<unsigned>(bin);
-        atomicAdd(&s_bin[bin], 1);
-    }
-    __syncthreads();
-    // exclusive prefix over the bins: kBins / kOrderThreads bins per thread
-    constexpr int kPer = kBins / kOrderThreads;
-    static_assert(kBins % kOrderThreads == 0, "bins split evenly over the CTA");
+    // exclusive prefix over the bins: kPer bins per thread
+    constexpr int kPer = kOrderBins / kOrderThreads;
     int acc = 0;
     for (int q = 0; q < kPer; ++q) acc += s_bin[threadIdx.x * kPer + q];
     s_part[threadIdx.x] = acc;
@@ -412,55 +404,123 @@ __device__ void write_block_order(unsigned* s_key, const int* start, int G, int 
         run += v;
     }
     __syncthreads();
-    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) out[atomicAdd(&s_bin[s_key[pos]], 1)] = pos;
+    if (!s_tmp) {
+        for (int pos = threadIdx.x; pos < m; pos += blockDim.x) out[atomicAdd(&s_bin[s_key[pos] >> 4], 1)] = pos;
+        return;
+    }
+    // entries (low key bits << 16 | pos): their order is the order wanted
+    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
+        const unsigned key = s_key[pos];
+        s_tmp[atomicAdd(&s_bin[key >> 4], 1)] = (key & 15u) << 16 | static_cast<unsigned>(pos);
+    }
+    __syncthreads();
+    // s_bin[b] is now the end of bin b
+    for (int b = threadIdx.x; b < kOrderBins; b += blockDim.x) {
+        const int lo = b == 0 ? 0 : s_bin[b - 1], hi = s_bin[b];
+        if (hi - lo > kOrderSortMax) continue;
+        for (int r = lo + 1; r < hi; ++r) {
+            const unsigned v = s_tmp[r];
+            int t = r;
+            while (t > lo && s_tmp[t - 1] > v) {
+                s_tmp[t] = s_tmp[t - 1];
+                --t;
+            }
+            s_tmp[t] = v;
+        }
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < m; r += blockDim.x) out[r] = static_cast<int>(s_tmp[r] & 0xffffu);
 }
 
-// Count order of one count group per CTA: key = the largest eps of the
-// group's pairs. Dynamic shared memory: m keys.
-__global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArgs A) {
+// Count order of one count group per CTA: boxes of the largest eps of the
+// group's pairs on the node grid. Dynamic shared memory: corder_ld keys,
+// then, with `sort_low`, corder_ld words for write_key_order's bins.
+__global__ void __launch_bounds__(kOrderThreads) grid_count_order_kernel(GridArgs A, int sort_low) {
     extern __shared__ unsigned s_key[];
+    __shared__ float s_t[2][16];
     const CountGroup grp = A.groups[blockIdx.x];
     const GridNode nd = A.nodes[grp.node];
     const float* eps = grp.side ? A.eps_b : A.eps_a;
-    const int m = nd.m, G = nd.G;
+    const int m = nd.m;
+    if (threadIdx.x < 32) {
+        const int L = threadIdx.x & 15;
+        const float* e = threadIdx.x < 16 ? nd.e1 : nd.e2;
+        s_t[threadIdx.x >> 4][L] = L < 15 ? e[2 * L + 1] : __int_as_float(0x7fc00000);
+    }
+    __syncthreads();
     long long o[kCountGroup];
 #pragma unroll
     for (int p = 0; p < kCountGroup; ++p) o[p] = A.pairs[grp.pairs[p]].scratch;  // unused slots repeat pairs[0]
+    // the grid's coordinates in storage order (coalesced)
+    const float* x1 = nd.sx + static_cast<long long>(nd.c1) * m;
+    const float* x2 = nd.c2 >= 0 ? nd.sx + static_cast<long long>(nd.c2) * m : nullptr;
     for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
         const int j = __ldg(nd.perm + pos);
         float e = __ldg(eps + o[0] + j);
 #pragma unroll
         for (int p = 1; p < kCountGroup; ++p) e = fmaxf(e, __ldg(eps + o[p] + j));
-        s_key[pos] = size_bits(e);
+        s_key[pos] = box_key(s_t[0], s_t[1], __ldg(x1 + pos), x2 ? __ldg(x2 + pos) : 0.f, e);
     }
-    const auto cell_of = [&](int pos, int& row, int& col) {
-        const int c = __ldg(nd.cell + __ldg(nd.perm + pos));
-        row = c / G;
-        col = c - row * G;
-    };
-    write_block_order(s_key, nd.start, G, m, cell_of, A.corder + static_cast<long long>(blockIdx.x) * A.corder_ld);
+    __syncthreads();
+    write_key_order(s_key, m, A.corder + static_cast<long long>(blockIdx.x) * A.corder_ld,
+                    sort_low ? s_key + A.corder_ld : nullptr);
 }
 
-// Search order of one pair per CTA: key = the larger of the two nodes' scale
-// estimates, which follows the k-th joint distance closely enough to group
-// queries with similar boxes. Dynamic shared memory: m keys.
+// Search order: cells in kOrderBlock x kOrderBlock blocks, blocks in Z
+// order, and within a block the queries by size class. Box Z codes of the
+// estimates, which serve the counts, made the search slower (197 against
+// 175 ms per 8192-pair batch at m = 10000): a warp's queries then spread
+// over more cells than its seed rectangle allows, and its lists fill later.
+constexpr int kOrderBlocks = (kGridMaxG + kOrderBlock - 1) / kOrderBlock;  // per axis
+constexpr int kOrderClasses = 64;
+static_assert(kOrderBlocks * kOrderBlocks * kOrderClasses == kOrderBins, "one counting-sort bin per class");
+
+__device__ __forceinline__ unsigned block_zcode(int bx, int by) {
+    unsigned z = 0;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) z |= ((bx >> b) & 1u) << (2 * b + 1) | ((by >> b) & 1u) << (2 * b);
+    return z;
+}
+
+// Size class of a box size e >= 0: its quarter octave (the float's exponent
+// and top two mantissa bits; +inf and NaN land in the top class).
+__device__ __forceinline__ unsigned size_bits(float e) {
+    return isnan(e) ? 0xffffffffu : __float_as_uint(fmaxf(e, 0.f)) >> 21;
+}
+
+// Search order of one pair per CTA: the size class of the larger of the two
+// nodes' scale estimates, which follows the k-th joint distance closely
+// enough to group queries with similar boxes; the smallest class present
+// becomes class 0. Dynamic shared memory: m keys.
 __global__ void __launch_bounds__(kOrderThreads) grid_pair_order_kernel(const KsgPairDesc* pairs,
                                                                        const GridPair* gps,
                                                                        const GridNode* nodes) {
     extern __shared__ unsigned s_key[];
+    __shared__ unsigned s_lo;
     const GridPair gp = gps[blockIdx.x];
     const GridNode na = nodes[gp.a], nb = nodes[gp.b];
     const int m = pairs[blockIdx.x].m, G = na.G;
+    if (threadIdx.x == 0) s_lo = 0xffffffffu;
+    __syncthreads();
+    unsigned lo = 0xffffffffu;
     for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
         const int j = __ldg(gp.perm + pos);
         s_key[pos] = size_bits(fmaxf(__ldg(na.est + j), __ldg(nb.est + j)));
+        lo = min(lo, s_key[pos]);
     }
-    const auto cell_of = [&](int pos, int& row, int& col) {
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    if ((threadIdx.x & 31) == 0) atomicMin(&s_lo, lo);
+    __syncthreads();
+    lo = s_lo;
+    for (int pos = threadIdx.x; pos < m; pos += blockDim.x) {
         const int j = __ldg(gp.perm + pos);
-        row = __ldg(na.cell + j) / G;
-        col = __ldg(nb.cell + j) / G;
-    };
-    write_block_order(s_key, gp.start, G, m, cell_of, gp.qpos);
+        const int row = __ldg(na.cell + j) / G, col = __ldg(nb.cell + j) / G;
+        const unsigned d = s_key[pos] - lo;
+        const unsigned cls = d < static_cast<unsigned>(kOrderClasses) ? d : kOrderClasses - 1;
+        s_key[pos] = (block_zcode(row / kOrderBlock, col / kOrderBlock) * kOrderClasses + cls) << 4;
+    }
+    __syncthreads();
+    write_key_order(s_key, m, gp.qpos, nullptr);
 }
 
 // One CTA per row.
@@ -487,11 +547,11 @@ template <int D>
 void launch_pass1(const GridArgs& a, int kmax, int grid, cudaStream_t st) {
     const dim3 b(32 * kGridWarps);
     switch (kmax) {
-        case 6: ksg_grid_pass1_kernel<D, 6><<<grid, b, 0, st>>>(a); break;
-        case 8: ksg_grid_pass1_kernel<D, 8><<<grid, b, 0, st>>>(a); break;
-        case 16: ksg_grid_pass1_kernel<D, 16><<<grid, b, 0, st>>>(a); break;
-        case 32: ksg_grid_pass1_kernel<D, 32><<<grid, b, 0, st>>>(a); break;
-        case 64: ksg_grid_pass1_kernel<D, 64><<<grid, b, 0, st>>>(a); break;
+        case 6: ksg_grid_pass1_kernel<D, 6, false><<<grid, b, 0, st>>>(a); break;
+        case 8: ksg_grid_pass1_kernel<D, 8, false><<<grid, b, 0, st>>>(a); break;
+        case 16: ksg_grid_pass1_kernel<D, 16, false><<<grid, b, 0, st>>>(a); break;
+        case 32: ksg_grid_pass1_kernel<D, 32, false><<<grid, b, 0, st>>>(a); break;
+        case 64: ksg_grid_pass1_kernel<D, 64, false><<<grid, b, 0, st>>>(a); break;
         default: fail(NSG_ERR_UNSUPPORTED, "no grid kernel for this k");
     }
 }
@@ -644,7 +704,11 @@ int grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* n
     return 1;
 }
 
-void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st) {
+void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, bool tie_record, cudaStream_t st) {
+    if (tie_record) {
+        grid_launch_search_rec(a, d, kmax, grid, st);
+        return;
+    }
     switch (d) {
         case 1: launch_pass1<1>(a, kmax, grid, st); break;
         case 2: launch_pass1<2>(a, kmax, grid, st); break;
@@ -657,11 +721,13 @@ void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream
 GridArgs grid_launch_count_order(const GridArgs& a, cudaStream_t st) {
     GridArgs c = a;
     if (c.corder && c.corder_ld <= kOrderMaxM && c.ngroups > 0) {
-        const size_t smem = sizeof(unsigned) * static_cast<size_t>(c.corder_ld);
+        // keys, and up to kOrderSortLowMaxM the bins' second copy
+        const int sort_low = c.corder_ld <= kOrderSortLowMaxM ? 1 : 0;
+        const size_t smem = sizeof(unsigned) * static_cast<size_t>(c.corder_ld) * (1 + sort_low);
         // set on every launch: the attribute belongs to the current device
         NSG_CUDA(cudaFuncSetAttribute(grid_count_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(sizeof(unsigned) * kOrderMaxM)));
-        grid_count_order_kernel<<<c.ngroups, kOrderThreads, smem, st>>>(c);
+        grid_count_order_kernel<<<c.ngroups, kOrderThreads, smem, st>>>(c, sort_low);
         NSG_CUDA(cudaGetLastError());
     } else {
         c.corder = nullptr;
@@ -701,7 +767,7 @@ int grid_search_ctas_per_sm(int d, int kmax) {
     int n = 0;
     const int b = 32 * kGridWarps;
     cudaError_t e = cudaSuccess;
-#define NSG_OCC(D_, K_) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ksg_grid_pass1_kernel<D_, K_>, b, 0)
+#define NSG_OCC(D_, K_) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ksg_grid_pass1_kernel<D_, K_, false>, b, 0)
     switch (d * 100 + kmax) {
         case 106: NSG_OCC(1, 6); break;
         case 108: NSG_OCC(1, 8); break;

@@ -168,13 +168,61 @@ __device__ __forceinline__ void stage_async(float* tile, int* jt, const float* s
     cp_async_commit();
 }
 
-// Pass 1 over a staged chunk: frames' original indices in jt. The list holds
-// the KN nearest frames other than the query itself, with the flag `tied`
-// for a frame outside it at the k-th distance (ksgk::admit).
+// What pass 1 knows about the frames outside a query's list at distance
+// U = its last entry, kept in shared memory (rarely touched, so it costs no
+// registers in the scan): tr[0] the U the record was made at, tr[kTieStride]
+// and tr[2 * kTieStride] the marginal pair all those frames share, or
+// kTieMixed (marginals are never negative) when they differ. U only
+// decreases and no frame can lie outside the list at a new, smaller U; a
+// record made at another U is stale. Every frame at the final U outside the
+// final list was offered while U had that value (rejected at v == U, or
+// pushed out of the last slot by a nearer frame with the last entry still
+// at U), so at the end a record made at the final U covers all of them.
+constexpr int kTieStride = 32 * kGridWarps;
+constexpr float kTieMixed = -2.f;
+
+__device__ __forceinline__ void tie_note(float* tr, float u, float va, float vb) {
+    if (tr[0] != u) {
+        tr[0] = u;
+        tr[kTieStride] = va;
+        tr[2 * kTieStride] = vb;
+    } else if (va != tr[kTieStride] || vb != tr[2 * kTieStride]) {
+        tr[kTieStride] = kTieMixed;
+    }
+}
+
+// Offer frame j (joint distance v, marginals va, vb) to the list: the first
+// frame at distance 0 stands for the query itself; a nearer frame enters
+// (ksgk::list_insert); one at U is recorded. A frame pushed out of the list
+// while U stays the same is recorded with its marginals read from the pair's
+// original rows. Callers offer only frames with v <= U.
 template <int D, int KN>
+__device__ __forceinline__ void admit_rec(float (&bd)[KN], int (&bj)[KN], bool& self_seen, float* tr, float v,
+                                          float va, float vb, int j, const float (&qa)[D], const float (&qb)[D],
+                                          const KsgPairDesc* P) {
+    const float u = bd[KN - 1];
+    if (v == 0.f && !self_seen) {
+        self_seen = true;
+    } else if (v < u) {
+        const int out = bj[KN - 1];
+        ksgk::list_insert<KN>(bd, bj, v, j);
+        if (bd[KN - 1] == u && out >= 0) {
+            tie_note(tr, u, ksgk::marginal_at<D>(qa, P->xa, P->ld, out), ksgk::marginal_at<D>(qb, P->xb, P->ld, out));
+        }
+    } else {
+        tie_note(tr, u, va, vb);
+    }
+}
+
+// Pass 1 over a staged chunk: frames' original indices in jt. The list holds
+// the KN nearest frames other than the query itself. Without REC the flag
+// `tied` says whether a frame outside it lies at its last distance
+// (ksgk::admit); with REC, tr records those frames' marginals (admit_rec).
+template <int D, int KN, bool REC>
 __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, int n,
                                             const float (&qa)[D], const float (&qb)[D],
-                                            float (&bd)[KN], int (&bj)[KN], bool& self_seen, bool& tied) {
+                                            float (&bd)[KN], int (&bj)[KN], bool& self_seen, bool& tied,
+                                            float* tr, const KsgPairDesc* P) {
     const int ngroups = (n + 3) >> 2;
     for (int g = 0; g < ngroups; ++g) {
         float4 ga[D], gb[D];
@@ -194,18 +242,31 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
             // of the warp inserts in a large share of groups. Insert each
             // lane's nearest frame of the group first, in one shared step;
             // it lowers the bound, so the other frames rarely still pass.
+            // (A loop offering the frames nearest first through one copy of
+            // the insertion ran 10% slower.)
             int fm = 0;
-            float vm = dz[0];
+            float vm = dz[0], am = da[0], bm = db[0];
 #pragma unroll
             for (int f = 1; f < 4; ++f) {
                 const bool lt = dz[f] < vm;
                 vm = lt ? dz[f] : vm;
                 fm = lt ? f : fm;
+                if constexpr (REC) {
+                    am = lt ? da[f] : am;
+                    bm = lt ? db[f] : bm;
+                }
             }
-            ksgk::admit<KN>(bd, bj, self_seen, tied, mn, jt[4 * g + fm]);
+            if constexpr (REC) admit_rec<D, KN>(bd, bj, self_seen, tr, mn, am, bm, jt[4 * g + fm], qa, qb, P);
+            else ksgk::admit<KN>(bd, bj, self_seen, tied, mn, jt[4 * g + fm]);
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
-                if (f != fm && dz[f] <= bd[KN - 1]) ksgk::admit<KN>(bd, bj, self_seen, tied, dz[f], jt[4 * g + f]);
+                if (f != fm && dz[f] <= bd[KN - 1]) {
+                    if constexpr (REC) {
+                        admit_rec<D, KN>(bd, bj, self_seen, tr, dz[f], da[f], db[f], jt[4 * g + f], qa, qb, P);
+                    } else {
+                        ksgk::admit<KN>(bd, bj, self_seen, tied, dz[f], jt[4 * g + f]);
+                    }
+                }
             }
         }
     }
@@ -265,11 +326,18 @@ __device__ __forceinline__ void tie_chunk(const float* tile, int n, const float 
 }  // namespace gridk
 
 // ---- pass 1: joint k nearest neighbours, eps, ties -----------------------------
-template <int D, int KMAX>
+// REC: ties checked through the shared-memory tie record (gridk::tie_note)
+// rather than by scanning the frames within the k-th distance again after
+// the search. The record costs registers in the scan (7 ms more per
+// 8192-pair batch at m = 10000), the scan costs little where ties are rare,
+// so REC serves plans of resampled trajectories, where copies of one frame
+// tie on a large share of samples (a quarter less search time there).
+template <int D, int KMAX, bool REC>
 __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid_pass1_kernel(GridArgs A) {
     using namespace gridk;
     __shared__ __align__(16) float s_tile[kGridWarps][2 * D * kGridChunk];
     __shared__ int s_jt[kGridWarps][kGridChunk];
+    __shared__ float s_tie[REC ? 3 * kTieStride : 1];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     float* tile = s_tile[wid];
@@ -304,6 +372,8 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
         float bd[KL];
         int bj[KL];
         bool self_seen = false, tied = false;
+        float* tr = s_tie + (REC ? threadIdx.x : 0);
+        if constexpr (REC) tr[0] = -1.f;  // no record
         const int nsent = KMAX - (A.k + 2);
 #pragma unroll
         for (int s = 0; s < KL; ++s) {
@@ -416,8 +486,8 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
                         cp_async_wait<0>();
                     }
                     __syncwarp();
-                    pass1_chunk<D, KL>(tile + 64 * half, jt + 64 * half, min(64, hi - lo - 64 * ci), qa, qb, bd,
-                                       bj, self_seen, tied);
+                    pass1_chunk<D, KL, REC>(tile + 64 * half, jt + 64 * half, min(64, hi - lo - 64 * ci), qa, qb,
+                                            bd, bj, self_seen, tied, tr, P);
                     __syncwarp();
                 }
             }
@@ -427,18 +497,27 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
         }
         // eps from list positions 1..k (original rows), tie test
         float ea = 0.f, eb = 0.f;
-        // wk: the k-th distance; a tie when another frame lies at wk too
+        // wk: the k-th distance. A tie when another frame lies at wk too and
+        // the frames at wk do not all have the same marginal pair; when they
+        // do, whichever of them the reference's sort puts first gives the
+        // same eps, and the search's result stands.
         const float wk = bd[KL - 1];
-        bool tie = valid && tied && wk > 0.f;
+        bool tie = valid && (REC ? tr[0] == wk : tied) && wk > 0.f;
         if (valid) {
+            const float ta = REC ? tr[kTieStride] : 0.f, tb = REC ? tr[2 * kTieStride] : 0.f;
+            bool same = ta >= 0.f;
 #pragma unroll
             for (int s = 0; s < KL; ++s) {
                 const int j = bj[s];
                 if (s >= nsent && j >= 0 && j < m) {
-                    ea = fmaxf(ea, ksgk::marginal_at<D>(qa, P->xa, P->ld, j));
-                    eb = fmaxf(eb, ksgk::marginal_at<D>(qb, P->xb, P->ld, j));
+                    const float da = ksgk::marginal_at<D>(qa, P->xa, P->ld, j);
+                    const float db = ksgk::marginal_at<D>(qb, P->xb, P->ld, j);
+                    ea = fmaxf(ea, da);
+                    eb = fmaxf(eb, db);
+                    if (REC && bd[s] == wk) same = same && da == ta && db == tb;
                 }
             }
+            if (REC) tie = tie && !same;
             const long long o = P->scratch + i;
             A.eps_a[o] = ea;
             A.eps_b[o] = eb;
@@ -446,37 +525,36 @@ __global__ void __launch_bounds__(32 * kGridWarps, (KMAX <= 8 ? 4 : 1)) ksg_grid
             if (A.eps_y) A.eps_y[o] = eb;
             if (A.kdist) A.kdist[o] = wk;
         }
-        if (__any_sync(0xffffffffu, tie)) {
-            // Frames at distance wk lie in the cells within wk of the sample.
-            // When they all have the same marginal pair, whichever of them the
-            // reference's sort puts first gives the same eps, and the search's
-            // result stands; only the others go to the tie kernel. Resampled
-            // trajectories (bootstrap) tie on a large share of samples, nearly
-            // all between copies of one frame.
-            int qrlo = G, qrhi = -1, qclo = G, qchi = -1;
-            if (tie) {
-                bin_range(na.e1, G, qa1, wk, qrlo, qrhi);
-                bin_range(nb.e1, G, qb1, wk, qclo, qchi);
-            }
-            const int rlo = __reduce_min_sync(0xffffffffu, qrlo);
-            const int rhi = __reduce_max_sync(0xffffffffu, qrhi);
-            float lo_a = inf_f(), hi_a = -inf_f(), lo_b = inf_f(), hi_b = -inf_f();
-            for (int cx = rlo; cx <= rhi; ++cx) {
-                const bool in_row = cx >= qrlo && cx <= qrhi;
-                const int clo = __reduce_min_sync(0xffffffffu, in_row ? qclo : G);
-                const int chi = __reduce_max_sync(0xffffffffu, in_row ? qchi : -1);
-                if (clo > chi) continue;
-                const int lo = __ldg(gp.start + cx * G + clo);
-                const int hi = __ldg(gp.start + cx * G + chi + 1);
-                for (int base = lo; base < hi; base += kGridChunk) {
-                    const int n = min(kGridChunk, hi - base);
-                    __syncwarp();
-                    stage<2 * D, false>(tile, nullptr, gp.sx, st, nullptr, base, n, lane);
-                    __syncwarp();
-                    tie_chunk<D>(tile, n, qa, qb, tie ? wk : -1.f, lo_a, hi_a, lo_b, hi_b);
+        if constexpr (!REC) {
+            if (__any_sync(0xffffffffu, tie)) {
+                // Frames at distance wk lie in the cells within wk of the
+                // sample: every tied lane takes the range of both marginals
+                // over the frames at exactly wk.
+                int qrlo = G, qrhi = -1, qclo = G, qchi = -1;
+                if (tie) {
+                    bin_range(na.e1, G, qa1, wk, qrlo, qrhi);
+                    bin_range(nb.e1, G, qb1, wk, qclo, qchi);
                 }
+                const int rlo = __reduce_min_sync(0xffffffffu, qrlo);
+                const int rhi = __reduce_max_sync(0xffffffffu, qrhi);
+                float lo_a = inf_f(), hi_a = -inf_f(), lo_b = inf_f(), hi_b = -inf_f();
+                for (int cx = rlo; cx <= rhi; ++cx) {
+                    const bool in_row = cx >= qrlo && cx <= qrhi;
+                    const int clo = __reduce_min_sync(0xffffffffu, in_row ? qclo : G);
+                    const int chi = __reduce_max_sync(0xffffffffu, in_row ? qchi : -1);
+                    if (clo > chi) continue;
+                    const int lo = __ldg(gp.start + cx * G + clo);
+                    const int hi = __ldg(gp.start + cx * G + chi + 1);
+                    for (int base = lo; base < hi; base += kGridChunk) {
+                        const int n = min(kGridChunk, hi - base);
+                        __syncwarp();
+                        stage<2 * D, false>(tile, nullptr, gp.sx, st, nullptr, base, n, lane);
+                        __syncwarp();
+                        tie_chunk<D>(tile, n, qa, qb, tie ? wk : -1.f, lo_a, hi_a, lo_b, hi_b);
+                    }
+                }
+                tie = tie && !(lo_a == hi_a && lo_b == hi_b);
             }
-            tie = tie && !(lo_a == hi_a && lo_b == hi_b);
         }
         // tied samples of the warp take consecutive slots of the tie list
         const unsigned tmask = __ballot_sync(0xffffffffu, tie);

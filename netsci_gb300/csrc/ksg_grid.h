@@ -108,12 +108,16 @@ struct GridArgs {
     int search_order;
 };
 
-// Block orders of queries: a grid's cells in kOrderBlock x kOrderBlock
-// blocks, blocks in Z order, and within a block the queries by a key of
-// their box size, so that a warp's queries share a block and have boxes of
-// similar size. Counts: the largest eps of the group's pairs. Search: the
-// larger of the two nodes' scale estimates. Built when m <= kOrderMaxM (the
-// keys of one grid fit in shared memory).
+// Query orders, built when m <= kOrderMaxM (the keys of one grid fit in
+// shared memory):
+//   * counts: the queries of the node grid sorted by the Z code of the box
+//     of cells their count box (the largest eps of the group's pairs)
+//     overlaps, its four corner cells at kOrderBits bits each, so that a
+//     warp's queries have boxes of nearly the same cells;
+//   * search: the pair grid's cells in kOrderBlock x kOrderBlock blocks,
+//     blocks in Z order, and within a block the queries by a size class of
+//     the larger of the two nodes' scale estimates.
+constexpr int kOrderBits = 4;
 constexpr int kOrderBlock = 4;
 constexpr int kOrderMaxM = 40960;
 // Orders are built for batches whose search runs at least this many waves
@@ -156,7 +160,13 @@ void grid_launch_nodes(GridNode* nodes, int nnodes, int d, bool est, cudaStream_
 // GridArgs::search_order for the batch.
 int grid_launch_pairs(const KsgPairDesc* pairs, GridPair* gps, const GridNode* nodes, int npairs,
                       int max_m, int d, bool order, cudaStream_t st);
-void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st);
+// The search; tie_record: ties checked through a record kept during the
+// scan (grid_launch_search_rec, ksg_grid_rec.cu) instead of a second scan of
+// the frames within each tied query's k-th distance. Plans of resampled
+// trajectories take it: copies of one frame tie on a large share of their
+// samples.
+void grid_launch_search(const GridArgs& a, int d, int kmax, int grid, bool tie_record, cudaStream_t st);
+void grid_launch_search_rec(const GridArgs& a, int d, int kmax, int grid, cudaStream_t st);
 void grid_launch_counts(const GridArgs& a, int d, int grid, cudaStream_t st);
 // The two halves of grid_launch_counts: the count-order kernel (when the
 // args carry a count order; returns the args the count kernel takes), then

@@ -30,7 +30,7 @@ namespace nsg {
 namespace {
 
 constexpr int kWarpsPerCta = 8;
-constexpr int kCtasPerSm = 4;  // latency-bound: as many warps as 64 registers allow
+constexpr int kCtasPerSm = 6;  // latency-bound: 48 warps per SM (40 registers) replays about 6% faster than 32
 constexpr int kStack = 64;
 constexpr unsigned kFull = 0xffffffffu;
 

@@ -463,7 +463,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     a.corder = order ? d_corder_.as<int>() : nullptr;
     a.corder_ld = maxm;
     const int sms = sm_count();
-    grid_launch_search(a, d, kmax, sms * grid_search_ctas_per_sm(d, kmax), s);
+    grid_launch_search(a, d, kmax, sms * grid_search_ctas_per_sm(d, kmax), false, s);
     a.counter = ctr + 1;
     grid_launch_counts(a, d, sms * grid_count_ctas_per_sm(d), s);
     grid_launch_combine(dp, static_cast<int>(np), a.cnt_a, a.cnt_b, psi_->as<float>(), d_scratch_.as<float>(),

@@ -94,6 +94,37 @@ def test_grid_and_exhaustive_agree_large(grid_search):
     assert np.array_equal(g.cpu().numpy(), e.cpu().numpy())
 
 
+@pytest.mark.parametrize("k", [6, 17])
+def test_grid_tie_record_matches_rescan(oracle_mod, grid_search, k):
+    """Resampled rows tie on many samples (copies of one frame). A plan of
+    frame-mapped pairs checks ties through the record kept during the scan;
+    a plan of the same rows copied out by hand checks them by scanning again.
+    Both must list the same tied samples and give the oracle's MI."""
+    from netsci_gb300 import device, synthetic
+    N, m = 5, 2300
+    X, _ = synthetic.protein_trajectory(N, m, seed=11)
+    Xd, mm = device.pack_trajectory(X, 3)
+    ab = synthetic.all_pairs(N)
+    idx = np.random.default_rng(12).integers(0, m, size=m).astype(np.int32)
+    fmap = torch.from_numpy(idx).cuda()
+    Xr = np.ascontiguousarray(X.reshape(N, 3, m)[:, :, idx].reshape(N, 3 * m))
+    Xrd, _ = device.pack_trajectory(Xr, 3)
+    out = []
+    for pairs in (device.make_pairs(Xd, mm, ab, fmap=fmap, m_samples=m), device.make_pairs(Xrd, mm, ab)):
+        mi = torch.empty(len(pairs), device="cuda")
+        plan = device.KsgPlan(pairs, k, 3, mi=mi)
+        assert plan.shape["search"] == "cell-grid"
+        plan.run()
+        torch.cuda.synchronize()
+        plan.check()
+        out.append((mi.cpu().numpy(), plan.tied_samples()))
+        plan.close()
+    expect = np.asarray(oracle_mod.pairs(Xr, m, 3, ab, k, gc=False, threads=8), np.float32)
+    assert np.array_equal(out[0][0], expect)
+    assert np.array_equal(out[1][0], expect)
+    assert out[0][1] == out[1][1]
+
+
 def test_grid_two_resamples_one_plan(oracle_mod, grid_search):
     """Pairs of two bootstrap resamples (two frame maps over the same rows)
     in one cell-grid plan: each resampled row is copied out once, and every
