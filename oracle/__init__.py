@@ -152,6 +152,8 @@ def ref_gpu_lib():
             fn.restype = ctypes.c_float
         G.refgpu_apsp_lengths.argtypes = [_f32p, _f32p, ctypes.c_int, ctypes.c_int]
         G.refgpu_apsp_lengths.restype = None
+        G.refgpu_row_stats.argtypes = [_f32p, ctypes.c_int, ctypes.c_int, _f32p, _f32p, _f32p]
+        G.refgpu_row_stats.restype = None
         _REF_GPU = G
     return _REF_GPU
 
@@ -163,6 +165,17 @@ def ref_gpu_apsp_lengths(A, max_path_length: int) -> np.ndarray:
     H = np.zeros_like(A)
     ref_gpu_lib().refgpu_apsp_lengths(A.ravel(), H.ravel(), A.shape[0], int(max_path_length))
     return H
+
+
+def ref_gpu_row_stats(a):
+    """The reference's row means (mean) and, from standardDeviation, its row
+    means and population standard deviations, GPU platform
+    (math_utils.cpp:6-36, math_utils_gpu.cu:22-198); a is m x n."""
+    a = _c(a, np.float32)
+    m, n = a.shape
+    u, u2, s = (np.zeros(m, np.float32) for _ in range(3))
+    ref_gpu_lib().refgpu_row_stats(a.ravel(), m, n, u, u2, s)
+    return u, u2, s
 
 
 def ref_pairs_checkpoint(X, n: int, d: int, ab, k: int, gc: bool, frequency: int,

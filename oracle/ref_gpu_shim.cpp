@@ -2,16 +2,18 @@
 //
 // C entry points over the reference's own, unmodified GPU functions
 // (netcalc/src/mutual_information_gpu.cu, generalized_correlation_gpu.cpp,
-// hedetniemi_gpu.cu), compiled for sm_103a by oracle/Makefile (target
-// `ref-gpu`) into oracle/_ref/libnetcalc_ref_gpu.so. Tests use them to pin
-// the shortest-path solver against the reference kernel, and bench.py times
-// them as the reference's GPU per-call path. Never linked by the product.
+// hedetniemi_gpu.cu, math_utils_gpu.cu), compiled for sm_103a by
+// oracle/Makefile (target `ref-gpu`) into oracle/_ref/libnetcalc_ref_gpu.so.
+// Tests use them to pin the shortest-path solver and the row statistics
+// against the reference kernels, and bench.py times them as the reference's
+// GPU per-call path. Never linked by the product.
 
 #include <cstring>
 
 #include "cuarray.h"
 #include "generalized_correlation.h"
 #include "hedetniemi.h"
+#include "math_utils.h"
 #include "mutual_information.h"
 
 namespace {
@@ -56,6 +58,25 @@ void refgpu_apsp_lengths(const float* A, float* H, int n, int max_path_length) {
     std::memcpy(H, h->host(), sizeof(float) * (size_t)n * n);
     delete h;
     delete a;
+}
+
+// mean and standardDeviation on the GPU platform (netcalc/src/math_utils.cpp:6-36,
+// math_utils_gpu.cu:22-198): a is m x n row-major; row means from both
+// calls, population standard deviations from the second.
+void refgpu_row_stats(const float* a, int m, int n, float* u_mean, float* u_sd, float* sigma) {
+    CuArray<float>* A = copy_in(a, m, n);
+    auto* u = new CuArray<float>;
+    mean(A, u, m, n, 0);
+    std::memcpy(u_mean, u->host(), sizeof(float) * (size_t)m);
+    delete u;
+    auto* u2 = new CuArray<float>;
+    auto* s = new CuArray<float>;
+    standardDeviation(A, u2, s, m, n, 0);
+    std::memcpy(u_sd, u2->host(), sizeof(float) * (size_t)m);
+    std::memcpy(sigma, s->host(), sizeof(float) * (size_t)m);
+    delete s;
+    delete u2;
+    delete A;
 }
 
 }  // extern "C"

@@ -12,6 +12,8 @@ into baseline/_ref/netsci).
   launch count covers the Jacobi iteration's convergence step count. There
   the reference's lengths must equal this library's bit for bit, on integer
   and on float weights.
+* Row statistics: the reference's mean and standard-deviation kernels sum in
+  the order this library restates, so their outputs must be equal bit for bit.
 * Mutual information: the reference's GPU per-pair call on tie-free inputs
   equals its CPU path (which the oracle restates), so it must equal this
   library's value too.
@@ -87,3 +89,25 @@ def test_mi_equals_reference_gpu_call(ref_gpu, golden):
         xa.fromNumpy1D(X[a])
         xb.fromNumpy1D(X[b])
         assert netcalc.generalizedCorrelationGpu(Xa=xa, Xb=xb, k=6, n=1000, xd=2, d=3) == ref_gc
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (3, 7), (5, 1023), (4, 1024), (6, 1025), (40, 3000),
+                                 (2, 70001)])
+def test_row_stats_equal_reference_kernels(ref_gpu, m, n):
+    """netcalc mean / standardDeviation (GPU platform) against the reference's
+    own meanKernel / standardDeviationKernel (math_utils_gpu.cu:22-158): the
+    same summation order, so bit for bit."""
+    import cuarray
+    import netcalc
+    rng = np.random.default_rng(m * 11 + n)
+    a = (rng.standard_normal((m, n)) * 5 + rng.uniform(-50, 50, (m, 1))).astype(np.float32)
+    ru, ru2, rs = ref_gpu.ref_gpu_row_stats(a)
+    A = cuarray.FloatCuArray()
+    A.fromNumpy2D(a)
+    u = cuarray.FloatCuArray()
+    netcalc.mean(A, u, m, n, netcalc.GPU_PLATFORM)
+    u2, s = cuarray.FloatCuArray(), cuarray.FloatCuArray()
+    netcalc.standardDeviation(A, u2, s, m, n, netcalc.GPU_PLATFORM)
+    assert np.array_equal(u.toNumpy1D(), ru)
+    assert np.array_equal(u2.toNumpy1D(), ru2)
+    assert np.array_equal(s.toNumpy1D(), rs)
