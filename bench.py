@@ -692,7 +692,7 @@ def main():
         e2e = {"value": world * args.steps * B / dt, "unit": "pairs/s",
                "h2d_bytes_per_step": int(X.nbytes + B * 2 * 4),
                "d2h_bytes_per_step": int(B * 4),
-               "api": "netcalc.generalizedCorrelation over host CuArrays (pageable host memory)"}
+               "api": "netcalc.generalizedCorrelation over host CuArrays (page-locked storage, as CuArray allocates arrays of 16 MB and more)"}
         last = R.toNumpy1D()
         assert np.array_equal(last, outs[S - 1].cpu().numpy()) or \
             np.max(np.abs(last - outs[S - 1].cpu().numpy())) <= 1e-6

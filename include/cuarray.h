@@ -69,8 +69,14 @@ public:
 
 private:
     void release();
+    // Host storage of `count` elements: page-locked (cudaHostAlloc) from
+    // kPinnedMinBytes up when a CUDA device is present, so host<->device
+    // copies of large arrays run at the link's speed; else new[].
+    T* alloc_host(size_t count);
+    void free_host();
     T* host_;
     T* device_;
+    T* pinned_ = nullptr;  // host_ came from cudaHostAlloc (freed with cudaFreeHost)
     int n_{};
     int m_{};
     int size_{};

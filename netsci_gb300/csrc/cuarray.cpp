@@ -23,9 +23,42 @@ CuArray<T>::~CuArray() {
     release();
 }
 
+namespace {
+// Arrays at least this large get page-locked host storage.
+constexpr size_t kPinnedMinBytes = size_t(16) << 20;
+}  // namespace
+
+template <typename T>
+T* CuArray<T>::alloc_host(size_t count) {
+    if (count == 0) count = 1;
+    const size_t bytes = count * sizeof(T);
+    if (bytes >= kPinnedMinBytes) {
+        void* p = nullptr;
+        if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) == cudaSuccess) {
+            pinned_ = static_cast<T*>(p);
+            return pinned_;
+        }
+        cudaGetLastError();  // no device: ordinary memory
+    }
+    pinned_ = nullptr;
+    return new T[count];
+}
+
+template <typename T>
+void CuArray<T>::free_host() {
+    if (pinned_) {
+        cudaFreeHost(pinned_);
+        pinned_ = nullptr;
+    } else if (host_) {
+        delete[] host_;
+    }
+    host_ = nullptr;
+}
+
 template <typename T>
 void CuArray<T>::release() {
-    if (allocatedHost_ && owner_ && host_) delete[] host_;
+    if (allocatedHost_ && owner_ && host_) free_host();
+    pinned_ = nullptr;
     if (allocatedDevice_ && device_) cudaFree(device_);
     host_ = nullptr;
     device_ = nullptr;
@@ -42,7 +75,7 @@ CuArrayError CuArray<T>::init(int m, int n) {
     size_ = m * n;
     bytes_ = static_cast<size_t>(size_) * sizeof(T);
     owner_ = 1;
-    host_ = new T[size_ > 0 ? size_ : 1];
+    host_ = alloc_host(static_cast<size_t>(size_));
     std::fill(host_, host_ + size_, T(0));
     allocatedHost_ = 1;
     return 0;
@@ -57,7 +90,7 @@ CuArrayError CuArray<T>::init(T* host, int m, int n) {
     size_ = m * n;
     bytes_ = static_cast<size_t>(size_) * sizeof(T);
     owner_ = 1;
-    host_ = new T[size_ > 0 ? size_ : 1];
+    host_ = alloc_host(static_cast<size_t>(size_));
     if (size_) std::copy(host, host + size_, host_);
     allocatedHost_ = 1;
     return 0;
@@ -83,10 +116,17 @@ template <typename T>
 CuArrayError CuArray<T>::fromCuArrayDeepCopy(CuArray<T>* src, int start, int end, int m, int n) {
     if (!src || start < 0 || end < start || end >= src->m_) return 1;
     if ((end - start + 1) * src->n_ != m * n) return 1;
-    T* copy = new T[m * n > 0 ? m * n : 1];
+    // the new storage is filled before this array's own is released (src may
+    // be this array)
+    T* const old_pinned = pinned_;
+    pinned_ = nullptr;
+    T* copy = alloc_host(static_cast<size_t>(m) * n);
+    T* const copy_pinned = pinned_;
     std::copy(src->host_ + static_cast<size_t>(start) * src->n_,
               src->host_ + static_cast<size_t>(end + 1) * src->n_, copy);
+    pinned_ = old_pinned;
     release();
+    pinned_ = copy_pinned;
     owner_ = 1;
     m_ = m;
     n_ = n;
@@ -119,7 +159,7 @@ CuArrayError CuArray<T>::allocatedDevice() const { return allocatedDevice_; }
 template <typename T>
 CuArrayError CuArray<T>::allocateHost() {
     if (!allocatedHost_ && owner_) {
-        host_ = new T[size_ > 0 ? size_ : 1];
+        host_ = alloc_host(static_cast<size_t>(size_));
         allocatedHost_ = 1;
     }
     return allocatedHost_ ? 0 : 1;
@@ -166,8 +206,7 @@ CuArrayError CuArray<T>::toHost() {
 template <typename T>
 CuArrayError CuArray<T>::deallocateHost() {
     if (allocatedHost_ && owner_) {
-        delete[] host_;
-        host_ = nullptr;
+        free_host();
         allocatedHost_ = 0;
     }
     return allocatedHost_ ? 1 : 0;
