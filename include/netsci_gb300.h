@@ -229,11 +229,14 @@ int nsg_ksg_set_shape(int threads, int r, int frames, int variant);
 int nsg_ksg_set_staging(int staging);
 /* Search for later plans: 1 cell grids (ksg_grid.cuh: only the frames whose
  * cells can reach a query are evaluated; same results), 0 exhaustive, -1
- * automatic (cell grids when no pair has a frame map and at least half of
- * the work, counted as m^2 per pair, is in pairs with m >= 1000). */
+ * automatic (cell grids when at least half of the work, counted as m^2 per
+ * pair, is in pairs with m >= 1000 (4000 for plans of fewer than 8 pairs)
+ * and the copies of frame-mapped rows, which the grids search instead of
+ * the maps, fit in 8 GiB). */
 int nsg_ksg_set_search(int mode);
-/* Query orders of later cell-grid plans: 1 = always build the block orders
- * (the search and count orders of a batch), 0 = never (cells in Z order),
+/* Query orders of later cell-grid plans: 1 = always build them (the search's
+ * block order and the counts' box order of a batch), 0 = never (cells in Z
+ * order),
  * -1 = automatic (only for batches whose search runs at least eight waves
  * of resident warps, where the order kernels pay for themselves). Orders
  * change which frames are visited first, never a result; m above 40960

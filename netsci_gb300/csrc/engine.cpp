@@ -621,7 +621,7 @@ struct KsgPlan::GridState {
     DeviceBuffer nodes, node_arena;       // GridNode[nnodes] and their buffers
     DeviceBuffer gps, pair_arena;         // GridPair per plan pair; pair grids of one batch
     std::vector<int> batch_maxm;          // largest m of each batch
-    std::vector<char> batch_order;        // whether each batch builds block orders
+    std::vector<char> batch_order;        // whether each batch builds query orders
     bool node_est = false;                // some batch does: nodes need scale estimates
     DeviceBuffer wprefix;                 // per batch: npairs+1 prefix of ceil(m/32)
     std::vector<long long> wprefix_off;   // offset of each batch's prefix

@@ -24,9 +24,11 @@
 //
 // Warps, not CTAs, own queries: a warp takes frames consecutive in a query
 // order as its queries (32 in pass 1, 16 at two lanes each in the counts).
-// The order is a block order where the batch builds one (4 x 4 cell blocks
-// in Z order, queries within a block by box size, ksg_grid.cu), else the Z
-// order of the cells. The queries' boxes then overlap. The warp streams the
+// Where the batch builds query orders (ksg_grid.cu), pass 1 takes a block
+// order (4 x 4 cell blocks in Z order, queries within a block by a size
+// class of their box) and the counts a box order (the Z code of the cells
+// their count box spans); else both take the Z order of the cells. The
+// queries' boxes then overlap. The warp streams the
 // frames of the cells it must visit through its own slice of shared memory,
 // read back as float4 (pass 1) or float2 (counts) broadcasts.
 // Pass 1 first scans the rectangle of cells its queries sit in (the seed,

@@ -429,7 +429,7 @@ bool Server::run_tick_grid(std::vector<std::pair<Job*, std::pair<long long, long
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         gpre[gi + 1] = gpre[gi] + (h_pairs_[groups[gi].pairs[0]].m + kCountQueries - 1) / kCountQueries;
     }
-    const bool order = grid_orders_pay(wacc, sm_count());  // block orders for this tick
+    const bool order = grid_orders_pay(wacc, sm_count());  // query orders for this tick
     if (order) ensure(d_corder_, sizeof(int) * std::max<size_t>(1, groups.size() * static_cast<size_t>(maxm)));
     NSG_CUDA(cudaMemcpyAsync(d_groups_.get(), groups.data(), sizeof(CountGroup) * groups.size(),
                              cudaMemcpyHostToDevice, s));

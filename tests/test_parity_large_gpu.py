@@ -12,7 +12,7 @@ CPU code), on:
   transform, bit-exact);
 * one pair at m = 24000, where a pair grid no longer fits the staged
   (shared-memory) build and is scattered straight to global memory;
-* one pair at m = 45000, above the largest m the block orders take (the
+* one pair at m = 45000, above the largest m the query orders take (the
   search and counts fall back to the Z order of cells);
 * the Gaussian MI requests of the serving mix at their largest size,
   n = 20000, d = 1, k = 4.
@@ -86,7 +86,7 @@ def test_c4_random_pairs_per_sample(c4_trajectory, c4_pairs, c4_oracle, knobs, s
 @pytest.mark.parametrize("orders", [1, 0, -1])
 def test_c4_random_pairs_one_plan(c4_trajectory, c4_pairs, c4_oracle, knobs, orders):
     """The bench's path: one autotuned, graph-replayed plan over the pairs,
-    with the block orders forced on, off, or left to the planner."""
+    with the query orders forced on, off, or left to the planner."""
     knobs.set_ksg_orders(orders)
     Xd, m = knobs.pack_trajectory(c4_trajectory, 3)
     mi = torch.empty(len(c4_pairs), device="cuda")
@@ -128,7 +128,7 @@ def test_large_m_pair_per_sample(oracle_mod, knobs, m, seed):
 
 
 def test_block_orders_at_their_largest_m_on_a_correlated_pair(oracle_mod, knobs):
-    """m = 40960, the largest m the block orders take, on a pair whose two
+    """m = 40960, the largest m the query orders take, on a pair whose two
     rows are nearly the same motion: its frames crowd the diagonal blocks of
     the pair grid, the case that made ranking a query against its whole
     block quadratic. The orders are built by counting sort now; every
