@@ -94,6 +94,35 @@ def test_grid_and_exhaustive_agree_large(grid_search):
     assert np.array_equal(g.cpu().numpy(), e.cpu().numpy())
 
 
+@pytest.mark.parametrize("d,k,n", [(1, 4, 3000), (2, 6, 2600), (3, 5, 2100)])
+def test_grid_query_orders_forced_match_oracle(oracle_mod, grid_search, d, k, n):
+    """Query orders forced on for small plans (the planner would skip them):
+    the search's block order and the counts' box order, for one, two and
+    three coordinates per node (one coordinate: node grids without a second
+    axis). Orders only change the scan, so MI equals the oracle's."""
+    from netsci_gb300 import device, synthetic
+    rng = np.random.default_rng(d * 100 + k)
+    N = 5
+    base = rng.standard_normal((N, d, n)).astype(np.float32)
+    mix = rng.standard_normal((N, N)).astype(np.float32) * 0.6
+    X = np.ascontiguousarray(np.einsum("ab,bcn->acn", mix, base).reshape(N, d * n))
+    ab = synthetic.all_pairs(N)
+    expect = np.asarray(oracle_mod.pairs(X, n, d, ab, k, gc=False, threads=8), np.float32)
+    device.set_ksg_orders(1)
+    try:
+        Xd, m = device.pack_trajectory(X, d)
+        mi = torch.empty(len(ab), device="cuda")
+        plan = device.KsgPlan(device.make_pairs(Xd, m, ab), k, d, mi=mi)
+        assert plan.shape["search"] == "cell-grid"
+        plan.run()
+        torch.cuda.synchronize()
+        plan.check()
+        plan.close()
+    finally:
+        device.set_ksg_orders(-1)
+    assert np.array_equal(mi.cpu().numpy(), expect)
+
+
 @pytest.mark.parametrize("k", [6, 17])
 def test_grid_tie_record_matches_rescan(oracle_mod, grid_search, k):
     """Resampled rows tie on many samples (copies of one frame). A plan of
