@@ -14,9 +14,10 @@
 // outside n x n, so padded k contribute nothing and no load needs a bound
 // check); the result is transposed back into H once at the end.
 //
-// Kernel shape: a 128 x 64 output tile per CTA of 256 threads, 8 x 4 outputs
-// per thread (two CTAs per SM). k runs in slabs of 16: both operand tiles
-// (128 and 64 rows of 16 floats) are copied into shared memory with 16-byte
+// Kernel shape: a 64 x 64 output tile per CTA of 256 threads, 4 x 4 outputs
+// per thread (four CTAs per SM, 64 registers; 128 x 64 tiles at 8 x 4 per
+// thread and two CTAs per SM took 12% longer). k runs in slabs of 16: both
+// operand tiles (64 rows of 16 floats each) are copied into shared memory with 16-byte
 // cp.async into two buffers, so the next slab loads while this one is
 // reduced. Rows are padded to 20 floats, which keeps the 16-byte reads of a
 // quarter-warp on distinct banks. Each thread reads four consecutive k of a
@@ -55,7 +56,7 @@
 namespace nsg {
 namespace {
 
-constexpr int kTileI = 128;  // output rows i per CTA (rows of X)
+constexpr int kTileI = 64;  // output rows i per CTA (rows of X)
 constexpr int kTileJ = 64;   // output columns j per CTA (rows of A)
 constexpr int kSlab = 16;    // k values per stage
 constexpr int kRow = 20;     // shared-memory row stride (floats)
@@ -70,7 +71,7 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, 4)
 hedetniemi_step_kernel(const float* __restrict__ X, const float* __restrict__ Ap,
                        float* __restrict__ Xn, int n, int P, int* changed, int step) {
     if (step > 0 && changed[step - 1] == 0) return;  // fixed point reached earlier
@@ -78,17 +79,17 @@ hedetniemi_step_kernel(const float* __restrict__ X, const float* __restrict__ Ap
     __shared__ __align__(16) float As[2][kTileJ][kRow];
     const float inf = __int_as_float(0x7f800000);
     const int tid = threadIdx.x;
-    // rows i = i0 + tx + 16u (u < 8), columns j = j0 + ty + 16v (v < 4)
+    // rows i = i0 + tx + 16u (u < 4), columns j = j0 + ty + 16v (v < 4)
     const int tx = tid & 15;
     const int ty = tid >> 4;
     const int i0 = blockIdx.y * kTileI;
     const int j0 = blockIdx.x * kTileJ;
     const float* xg = X + (size_t)i0 * P;
     const float* ag = Ap + (size_t)j0 * P;
-    // 128 + 64 rows of four 16-byte chunks: three chunks per thread
+    // 64 + 64 rows of four 16-byte chunks: two chunks per thread
     auto load_slab = [&](int buf, int k0) {
 #pragma unroll
-        for (int e = 0; e < 3; ++e) {
+        for (int e = 0; e < (4 * (kTileI + kTileJ)) / kThreads; ++e) {
             const int c = tid + kThreads * e;
             if (c < 4 * kTileI) {
                 const int r = c >> 2, q = c & 3;
@@ -102,9 +103,9 @@ hedetniemi_step_kernel(const float* __restrict__ X, const float* __restrict__ Ap
         cp_async_commit();
     };
 
-    float acc[8][4];
+    float acc[4][4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u)
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = inf;
 
@@ -121,13 +122,13 @@ hedetniemi_step_kernel(const float* __restrict__ X, const float* __restrict__ Ap
         const int b = sl & 1;
 #pragma unroll
         for (int kq = 0; kq < kSlab / 4; ++kq) {
-            float4 x[8], a[4];
+            float4 x[4], a[4];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) x[u] = *reinterpret_cast<const float4*>(&Xs[b][tx + 16 * u][4 * kq]);
+            for (int u = 0; u < 4; ++u) x[u] = *reinterpret_cast<const float4*>(&Xs[b][tx + 16 * u][4 * kq]);
 #pragma unroll
             for (int v = 0; v < 4; ++v) a[v] = *reinterpret_cast<const float4*>(&As[b][ty + 16 * v][4 * kq]);
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
+            for (int u = 0; u < 4; ++u)
 #pragma unroll
                 for (int v = 0; v < 4; ++v) {
                     const float2 s0 = nsg_add2(make_float2(x[u].x, x[u].y), make_float2(a[v].x, a[v].y));
@@ -141,7 +142,7 @@ hedetniemi_step_kernel(const float* __restrict__ X, const float* __restrict__ Ap
 
     bool diff = false;
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < 4; ++u) {
         const int i = i0 + tx + 16 * u;
         if (i >= n) continue;
 #pragma unroll
