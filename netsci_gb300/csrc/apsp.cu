@@ -16,11 +16,12 @@
 //
 // Kernel shape: a 64 x 64 output tile per CTA of 256 threads, 4 x 4 outputs
 // per thread (four CTAs per SM, 64 registers; 128 x 64 tiles at 8 x 4 per
-// thread and two CTAs per SM took 12% longer). k runs in slabs of 16: both
-// operand tiles (64 rows of 16 floats each) are copied into shared memory with 16-byte
-// cp.async into two buffers, so the next slab loads while this one is
-// reduced. Rows are padded to 20 floats, which keeps the 16-byte reads of a
-// quarter-warp on distinct banks. Each thread reads four consecutive k of a
+// thread and two CTAs per SM took 12% longer). k runs in slabs of 32 (16
+// took 6% longer: twice the barriers): both operand tiles (64 rows of 32
+// floats each) are copied into shared memory with 16-byte cp.async into two
+// buffers, so the next slab loads while this one is reduced. Rows are padded
+// to 36 floats, which keeps the 16-byte reads of a quarter-warp on distinct
+// banks. Each thread reads four consecutive k of a
 // row at once; one packed add (add.rn.f32x2) forms the sums for (k, k+1) and
 // one three-input min folds both into the running minimum: two instructions
 // per two (i, j, k) terms. The work is FADD/FMNMX issue-bound on CUDA cores;
@@ -58,8 +59,8 @@ namespace {
 
 constexpr int kTileI = 64;  // output rows i per CTA (rows of X)
 constexpr int kTileJ = 64;   // output columns j per CTA (rows of A)
-constexpr int kSlab = 16;    // k values per stage
-constexpr int kRow = 20;     // shared-memory row stride (floats)
+constexpr int kSlab = 32;    // k values per stage
+constexpr int kRow = 36;     // shared-memory row stride (floats)
 constexpr int kThreads = 256;
 constexpr int kPad = 128;    // P is a multiple of this (and of kTileJ, kSlab)
 
@@ -86,17 +87,19 @@ hedetniemi_step_kernel(const float* __restrict__ X, const float* __restrict__ Ap
     const int j0 = blockIdx.x * kTileJ;
     const float* xg = X + (size_t)i0 * P;
     const float* ag = Ap + (size_t)j0 * P;
-    // 64 + 64 rows of four 16-byte chunks: two chunks per thread
+    // 64 + 64 rows of eight 16-byte chunks: four chunks per thread
     auto load_slab = [&](int buf, int k0) {
 #pragma unroll
-        for (int e = 0; e < (4 * (kTileI + kTileJ)) / kThreads; ++e) {
+        constexpr int kChunks = kSlab / 4;  // 16-byte chunks per row
+        static_assert((kChunks * (kTileI + kTileJ)) % kThreads == 0, "whole chunks per thread");
+        for (int e = 0; e < (kChunks * (kTileI + kTileJ)) / kThreads; ++e) {
             const int c = tid + kThreads * e;
-            if (c < 4 * kTileI) {
-                const int r = c >> 2, q = c & 3;
+            if (c < kChunks * kTileI) {
+                const int r = c / kChunks, q = c % kChunks;
                 cp_async16(&Xs[buf][r][4 * q], xg + (size_t)r * P + k0 + 4 * q);
             } else {
-                const int c2 = c - 4 * kTileI;
-                const int r = c2 >> 2, q = c2 & 3;
+                const int c2 = c - kChunks * kTileI;
+                const int r = c2 / kChunks, q = c2 % kChunks;
                 cp_async16(&As[buf][r][4 * q], ag + (size_t)r * P + k0 + 4 * q);
             }
         }
