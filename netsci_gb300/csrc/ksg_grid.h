@@ -116,7 +116,7 @@ struct GridArgs {
 //     warp's queries have boxes of nearly the same cells;
 //   * search: the pair grid's cells in kOrderBlock x kOrderBlock blocks,
 //     blocks in Z order, and within a block the queries by a size class of
-//     the larger of the two nodes' scale estimates.
+//     the geometric mean of the two nodes' scale estimates.
 constexpr int kOrderBits = 4;
 constexpr int kOrderBlock = 4;
 constexpr int kOrderMaxM = 40960;
